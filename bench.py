@@ -1,0 +1,410 @@
+#!/usr/bin/env python3
+"""Benchmark of the FFT family on GB300 (one JSON line on stdout).
+
+Default workload: realft-based convolution and correlation of an N = 2^20
+real f64 signal (i.i.d. N(0,1)) with a 257-tap response (Gaussian window,
+sigma = m/6, times N(0,1)) stored in wrap-around order in a length-N buffer.
+One step = one convlv(isign=+1) call and one correl call.  The nominal work
+is 3 real FFTs per call, 2.5 N log2 N flops each.
+
+  value     GFLOP/s with inputs resident in HBM (device tensors through the
+            C ABI), CUDA events on the launching stream, L2 flushed (256 MiB
+            write) before every timed step
+  e2e       the same steps through the C ABI with pinned host buffers, the
+            host->device and device->host copies inside the timed region
+  roofline  the Stockham pass kernel: algorithmic bytes / its event-timed
+            duration against the measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle (a C++ restatement of the crate's routines)
+            on the host cores for a bounded sample of the same workload
+
+--impl reference times the CPU oracle alone (the reference crate itself
+cannot be built: no Rust toolchain, and its FFT modules are not compiled).
+Other workloads (--workload four1|batch|fourn|rlft3|large) exercise the other
+configurations; the driver runs the default.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FFT GFLOP/s (5N·log2N) & HBM GB/s vs peak; TC-split vs FP64 at rel-L2≤1e-6"
+FP64_PEAK_TFLOPS = 1.20  # DFMA loop measured on this machine's GB300 (probe recorded in the design doc)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="convlv",
+                    choices=["convlv", "four1", "batch", "fourn", "rlft3", "large"])
+    ap.add_argument("--form", default="fp64", choices=["fp64", "df64", "fp32"])
+    ap.add_argument("--no-forms", action="store_true", help="skip the extra precision forms")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    smax.append(float(p[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, p[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# distributed bookkeeping (one process per GPU; replicas of the workload)
+# ---------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def convlv_inputs():
+    from numrs_gb300 import workloads as W
+    x, r = W.convlv_c2()
+    y = W.normal(W.BASE_SEED + 21, x.size)
+    return x, r, y
+
+
+CONV_N = 1 << 20
+CONV_FLOPS = 2 * 3 * 2.5 * CONV_N * 20  # two calls, three real FFTs each
+
+
+def cpu_convlv_step(x, r, y):
+    import oracle as O
+    st, a = O.convlv(x, r, 1)
+    st2, b = O.correl(x, y)
+    assert st == 0 and st2 == 0
+    return a, b
+
+
+def cpu_baseline(seconds, x, r, y):
+    """Time the CPU oracle on whole steps for about `seconds` of work."""
+    import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    cpu_convlv_step(x, r, y)  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while True:
+        cpu_convlv_step(x, r, y)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 1000:
+            break
+    O.set_threads(1)
+    return {
+        "value": CONV_FLOPS * n / el / 1e9, "unit": "GFLOP/s", "cores": min(2, threads),
+        "kind": "port",
+        "sample": "%d whole steps (convlv + correl, N=2^20) in %.1f s; the two forward "
+                  "transforms of each call run on 2 threads as the reference's rayon::join "
+                  "does, the transforms themselves are serial as in the crate" % (n, el),
+    }
+
+
+def run_reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    x, r, y = convlv_inputs()
+    import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    for _ in range(max(0, min(args.warmup, 2))):
+        cpu_convlv_step(x, r, y)
+    t1 = time.perf_counter()
+    cpu_convlv_step(x, r, y)
+    per = time.perf_counter() - t1
+    budget = 90.0
+    steps = max(1, min(args.steps, int(budget / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        cpu_convlv_step(x, r, y)
+    el = time.perf_counter() - t0
+    val = CONV_FLOPS * steps / el / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "GFLOP/s", "n_gpus": args.gpus,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded N(0,1) signal, Gaussian-window response)",
+        "config": {"workload": "realft convlv + correl, N=2^20 real f64, m=257 taps in a "
+                               "length-N wrap-around buffer", "form": "fp64 (CPU)",
+                   "sampled_steps": steps, "requested_steps": args.steps},
+        "cpu_baseline": {"value": val, "unit": "GFLOP/s", "cores": min(2, threads), "kind": "port",
+                         "sample": "%d of %d requested steps, CPU oracle (C++ restatement of "
+                                   "Convolve.rs/Correlation.rs/Real_FT.rs)" % (steps, args.steps)},
+        "e2e": {"value": val, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    O.set_threads(1)
+    print(json.dumps(line), flush=True)
+
+
+def run_convlv(args, world, rank, local):
+    import torch
+    import numrs_gb300 as nr
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    x, r, y = convlv_inputs()
+    xd = torch.from_numpy(x).to(dev)
+    rd = torch.from_numpy(r).to(dev)
+    yd = torch.from_numpy(y).to(dev)
+    outa = torch.empty_like(xd)
+    outb = torch.empty_like(xd)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    form = args.form
+
+    def step(f=form):
+        nr.convlv(xd, rd, 1, form=f, out=outa)
+        nr.correl(xd, yd, form=f, out=outb)
+
+    nr.set_async(True)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    clocks = Clocks(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    nr.launch_count(reset=True)
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    launches = nr.launch_count()
+    clk = clocks.stop()
+    barrier(world)
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    total_ms = max_over_ranks(total_ms, world)
+    value = CONV_FLOPS * args.steps * world / (total_ms / 1e3) / 1e9
+
+    # ---- accuracy of this run against the CPU oracle ----
+    acc = {}
+    if rank == 0:
+        ra, rb = cpu_convlv_step(x, r, y)
+        ga, gb = outa.cpu().numpy(), outb.cpu().numpy()
+        acc[form] = max(np.linalg.norm(ga - ra) / np.linalg.norm(ra),
+                        np.linalg.norm(gb - rb) / np.linalg.norm(rb))
+
+    # ---- per-kernel event timing (a separate profiled repetition) ----
+    nprof = min(args.steps, 50)
+    nr.profile(True)
+    for i in range(nprof):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    pass_ms, pass_n, pass_bytes, pass_flops = nr.profile_read("pass")
+    tw_ms, tw_n, _, _ = nr.profile_read("twist")
+    sp_ms, sp_n, sp_bytes, _ = nr.profile_read("spectral")
+    nr.profile(False)
+
+    # ---- other precision forms, same step ----
+    forms = {}
+    if not args.no_forms and rank == 0:
+        for f in ("df64", "fp32"):
+            if f == form:
+                continue
+            for _ in range(3):
+                step(f)
+            torch.cuda.synchronize()
+            evs = []
+            for i in range(min(args.steps, 200)):
+                a0, b0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                flush.zero_()
+                a0.record(stream)
+                step(f)
+                b0.record(stream)
+                evs.append((a0, b0))
+            torch.cuda.synchronize()
+            ms = sum(a.elapsed_time(b) for a, b in evs)
+            ra, rb = cpu_convlv_step(x, r, y)
+            ga, gb = outa.cpu().numpy(), outb.cpu().numpy()
+            e = max(np.linalg.norm(ga - ra) / np.linalg.norm(ra),
+                    np.linalg.norm(gb - rb) / np.linalg.norm(rb))
+            forms[f] = {"value": CONV_FLOPS * len(evs) / (ms / 1e3) / 1e9, "unit": "GFLOP/s",
+                        "ms_per_step": ms / len(evs), "rel_l2_vs_fp64_oracle": e}
+    nr.set_async(False)
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    xh = torch.from_numpy(x).pin_memory().numpy()
+    rh = torch.from_numpy(r).pin_memory().numpy()
+    yh = torch.from_numpy(y).pin_memory().numpy()
+    oa = torch.empty(CONV_N, dtype=torch.float64).pin_memory().numpy()
+    ob = torch.empty(CONV_N, dtype=torch.float64).pin_memory().numpy()
+
+    def host_step():
+        nr.convlv(xh, rh, 1, form=form, out=oa)
+        nr.correl(xh, yh, form=form, out=ob)
+
+    for _ in range(3):
+        host_step()
+    e2e_steps = max(10, min(args.steps, 200))
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        host_step()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_val = CONV_FLOPS * e2e_steps * world / e2e_s / 1e9
+
+    if rank != 0:
+        return
+    hbm, hbm_kind = peaks()
+    pass_avg_ms = pass_ms / max(pass_n, 1)
+    achieved = (pass_bytes / max(pass_n, 1)) / (pass_avg_ms / 1e3) / 1e9 if pass_n else 0.0
+    cpu = cpu_baseline(args.cpu_seconds, x, r, y)
+    line = {
+        "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == "fp64" else form,
+        "data": "synthetic (seeded N(0,1) signal, Gaussian-window response)",
+        "config": {"workload": "realft convlv + correl, N=2^20 real f64, m=257 taps in a "
+                               "length-N wrap-around buffer; one step = one convlv and one correl",
+                   "form": form, "l2": "flushed between timed steps (256 MiB write)",
+                   "nominal_flops_per_step": CONV_FLOPS},
+        "e2e": {"value": e2e_val, "unit": "GFLOP/s", "steps": e2e_steps,
+                "h2d_bytes_per_step": 4 * CONV_N * 8, "d2h_bytes_per_step": 2 * CONV_N * 8,
+                "host_buffers": "pinned"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None,
+                     "kernel": "k_pass (Stockham pass)",
+                     "peak_source": "%s MEASURED_PEAKS.json hbm_gbs" % hbm_kind if hbm_kind == "measured"
+                     else "fallback 6.8 TB/s",
+                     "launches": pass_n, "avg_launch_ms": pass_avg_ms,
+                     "bytes_per_launch": pass_bytes / max(pass_n, 1)},
+        "compute_roofline": {"bound": "fp64" if form == "fp64" else "fp32",
+                             "achieved_tflops": pass_flops / (pass_ms / 1e3) / 1e12 if pass_ms else 0.0,
+                             "peak_tflops": FP64_PEAK_TFLOPS if form == "fp64" else 73.3,
+                             "note": "nominal 5 N log2 R per pass over the pass-kernel time; peaks "
+                                     "from the DFMA / FFMA probes"},
+        "kernels": {"pass": {"ms": pass_ms, "launches": pass_n},
+                    "twist": {"ms": tw_ms, "launches": tw_n},
+                    "spectral": {"ms": sp_ms, "launches": sp_n}, "profiled_steps": nprof},
+        "accuracy": {"rel_l2_vs_cpu_oracle": acc},
+        "forms": forms,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    if hbm_kind == "measured":
+        line["roofline"]["peak_source"] = "of measured (MEASURED_PEAKS.json hbm_gbs)"
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference_arm(args, world, rank)
+        return
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    if args.workload != "convlv":
+        raise SystemExit("workload %s is not wired into bench.py yet" % args.workload)
+    else:
+        run_convlv(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

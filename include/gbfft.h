@@ -1,0 +1,154 @@
+/*
+ * gbfft.h -- C ABI of the GB300 FFT library (libgbfft.so).
+ *
+ * Drop-in boundary for the FFT family of the numrs crate.  Each entry point
+ * replaces one Rust function of the crate; the crate's conventions are kept:
+ *
+ *   - data are interleaved f64 (re, im, re, im, ...) and transformed in place
+ *   - isign = +1 computes X_k = sum_j x_j exp(+2 pi i jk/N), isign = -1 the
+ *     conjugate sum; transforms are unnormalised
+ *   - realft packs Re X_{n/2} into data[1]; rlft3 returns the Nyquist plane in
+ *     speq; convlv takes its response in wrap-around order and scales by 2/n
+ *
+ * Arrays are 0-based.  Routines whose Rust versions take 1-based slices
+ * (cosft1, cosft2) take the 0-based array that starts at the crate's index 1.
+ *
+ * Every function returns a gbfft_status.  Pointers are host memory unless
+ * opts->device_ptrs is set.  Calls are synchronous for host pointers; for
+ * device pointers they are ordered on opts->stream (or the library stream)
+ * and synchronous unless opts->async is set.  The library is thread-safe
+ * (one internal lock).  No entry point changes any GPU setting.
+ */
+#ifndef GBFFT_H
+#define GBFFT_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GBFFT_OK = 0,
+  GBFFT_INVALID_ARG = 1,       /* bad isign, null pointer, length mismatch ...   */
+  GBFFT_UNSUPPORTED_SIZE = 2,  /* size is not a power of two or exceeds limits   */
+  GBFFT_CUDA_ERROR = 3,        /* a CUDA call failed; see gbfft_last_error()     */
+  GBFFT_TIMEOUT = 4,           /* a bounded device wait gave up                  */
+  GBFFT_OOM = 5,               /* device allocation failed                       */
+  /* convlv / correl error enums of the crate (Convolve.rs:226-238,
+   * Correlation.rs:389-399) */
+  GBFFT_EMPTY_INPUT = 10,
+  GBFFT_RESPONSE_TOO_LONG = 11,
+  GBFFT_INVALID_ISIGN = 12,
+  GBFFT_LENGTH_MISMATCH = 13,
+  GBFFT_ZERO_STD_DEV = 14
+} gbfft_status;
+
+/* Arithmetic form of a call. */
+typedef enum {
+  GBFFT_FORM_FP64 = 0,  /* IEEE double throughout (the crate's arithmetic)      */
+  GBFFT_FORM_FP32 = 1,  /* IEEE float arithmetic, f64 in and out               */
+  GBFFT_FORM_DF64 = 2   /* double-float (compensated FP32 pairs), f64 in/out    */
+} gbfft_form;
+
+typedef struct {
+  int form;          /* gbfft_form; 0 = FP64                                   */
+  int device_ptrs;   /* 1: all array arguments are device pointers             */
+  void* stream;      /* cudaStream_t for device-pointer calls, NULL = library  */
+  int async;         /* device-pointer calls only: 1 = do not synchronise      */
+} gbfft_opts;
+
+/* Library control ------------------------------------------------------- */
+int gbfft_init(int device);              /* optional; first call does it     */
+const char* gbfft_last_error(void);      /* message of the last failure      */
+int gbfft_version(void);                 /* 10000*major + 100*minor + patch  */
+/* Device scratch currently held by the library, in bytes. */
+size_t gbfft_scratch_bytes(void);
+/* Free cached plans, graphs and scratch (tables are kept). */
+int gbfft_release(void);
+/* Instrumentation (no counterpart in the crate).  Kernel launches issued
+ * since the last reset; optional event timing of every launch on its stream,
+ * summed per kind: 0 = FFT passes, 1 = realft twists, 2 = spectral products,
+ * 3 = other.  bytes = algorithmic bytes moved by those launches, flops =
+ * nominal 5 N log2 R of each radix-R pass over N points. */
+long long gbfft_launch_count(int reset);
+int gbfft_profile(int enable);  /* also clears the records */
+int gbfft_profile_read(int kind, double* ms, long long* launches, double* bytes,
+                       double* flops);
+
+/* Complex FFT ----------------------------------------------------------- */
+/* four1: src/FFT_1.rs:5 `pub fn four1(data: &mut [f64], nn: usize, isign: i32)`.
+ * data holds 2*nn doubles; nn a power of two <= 2^28. */
+int gbfft_four1(double* data, size_t nn, int isign, const gbfft_opts* opts);
+
+/* FFTProcessor::fft_batch: src/FFT_1.rs:185
+ * `pub fn fft_batch(&self, batches: &mut [&mut [f64]], isign: i32)`.
+ * count transforms, ptrs[t] holds 2*nn[t] doubles; sizes may differ. */
+int gbfft_four1_batch(double* const* ptrs, const size_t* nn, size_t count, int isign,
+                      const gbfft_opts* opts);
+
+/* Uniform batch: `count` transforms of nn points, `dist` doubles apart
+ * (dist >= 2*nn). */
+int gbfft_four1_many(double* data, size_t nn, size_t count, size_t dist, int isign,
+                     const gbfft_opts* opts);
+
+/* twofft: src/FFT_2.rs:3
+ * `pub fn twofft(data1: &[f64], data2: &[f64], fft1: &mut [f64], fft2: &mut [f64])`.
+ * data1, data2: n reals; fft1, fft2: 2n+2 doubles (the n-point spectra fill
+ * [0, 2n); the last two doubles are left as they are). */
+int gbfft_twofft(const double* data1, const double* data2, double* fft1, double* fft2,
+                 size_t n, const gbfft_opts* opts);
+
+/* Real FFT -------------------------------------------------------------- */
+/* realft: src/Real_FT.rs:4 `pub fn realft(data: &mut [f64], n: usize, isign: i32)`.
+ * n reals (power of two >= 2).  Forward output: data[0] = X_0,
+ * data[1] = X_{n/2}, data[2k], data[2k+1] = Re, Im X_k.  Inverse returns
+ * (n/2) x. */
+int gbfft_realft(double* data, size_t n, int isign, const gbfft_opts* opts);
+
+/* fourn: src/Fourn.rs:278 `fourn_simd(data: &mut [f64], nn: &[usize], ndim, isign)`
+ * with validate_inputs (src/Fourn.rs:367-378): ndim in 1..=nn_len, isign +-1,
+ * every nn[d] > 1.  Row-major, nn[ndim-1] contiguous. */
+int gbfft_fourn(double* data, const size_t* nn, size_t nn_len, size_t ndim, int isign,
+                const gbfft_opts* opts);
+
+/* rlft3: src/Real_FT3.rs:8 / rlft3_optimized :145
+ * `(data: &mut [f64], speq: &mut [f64], nn1, nn2, nn3, isign)`.
+ * data nn1*nn2*nn3 reals, speq nn1*2*nn2 doubles.  Inverse returns
+ * (nn1 nn2 nn3 / 2) x. */
+int gbfft_rlft3(double* data, double* speq, size_t nn1, size_t nn2, size_t nn3, int isign,
+                const gbfft_opts* opts);
+
+/* Sine and cosine transforms --------------------------------------------- */
+/* sinft (README.md:72, Numerical Recipes contract): y[0..n), y[0] taken as 0. */
+int gbfft_sinft(double* y, size_t n, const gbfft_opts* opts);
+/* cosft1: src/Cos_FT.rs:7 `cosft1(y: &mut [f64], n)`; y[0..n] (n+1 values). */
+int gbfft_cosft1(double* y, size_t n, const gbfft_opts* opts);
+/* cosft2: src/Cos_FT2.rs:7 `cosft2(y: &mut [f64], n, isign)`; y[0..n). */
+int gbfft_cosft2(double* y, size_t n, int isign, const gbfft_opts* opts);
+
+/* Spectral routines ------------------------------------------------------ */
+/* convlv: src/Convolve.rs:8
+ * `convlv(data: &[f64], respns: &[f64], isign: i32) -> Result<Array1<f64>, ConvlvError>`.
+ * data n reals, respns m <= n taps in wrap-around order, ans n reals.
+ * Errors: GBFFT_EMPTY_INPUT, GBFFT_RESPONSE_TOO_LONG, GBFFT_INVALID_ISIGN
+ * (checked in that order, Convolve.rs:13-21); n must be a power of two. */
+int gbfft_convlv(const double* data, size_t n, const double* respns, size_t m, int isign,
+                 double* ans, const gbfft_opts* opts);
+
+/* correl: src/Correlation.rs:8
+ * `correl(data1: &[f64], data2: &[f64]) -> Result<Array1<f64>, CorrelError>`.
+ * n <= 32 uses the reference's direct linear sum; larger n must be a power of
+ * two and gives the circular correlation. */
+int gbfft_correl(const double* data1, size_t n1, const double* data2, size_t n2, double* ans,
+                 const gbfft_opts* opts);
+
+/* magnitude_spectrum / power_spectrum: src/FFT_1.rs:206,218.  out[nn]. */
+int gbfft_magnitude_spectrum(const double* c, size_t nn, double* out, const gbfft_opts* opts);
+int gbfft_power_spectrum(const double* c, size_t nn, double* out, const gbfft_opts* opts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBFFT_H */

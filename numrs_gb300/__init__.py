@@ -1,0 +1,401 @@
+"""numrs_gb300 -- the FFT family of the numrs crate on one GB300.
+
+Python mirror of the crate's public FFT API over the C ABI of libgbfft.so
+(include/gbfft.h).  Names, argument meaning and error behaviour follow the
+Rust functions:
+
+    four1(data, nn, isign)                 src/FFT_1.rs:5
+    FFTProcessor().fft / .fft_batch        src/FFT_1.rs:143-190
+    twofft(data1, data2, fft1, fft2)       src/FFT_2.rs:3
+    realft(data, n, isign)                 src/Real_FT.rs:4
+    fourn(data, nn, ndim, isign)           src/Fourn.rs:278 (in-memory contract)
+    rlft3(data, speq, nn1, nn2, nn3, isign) src/Real_FT3.rs:8
+    cosft1(y, n), cosft2(y, n, isign), sinft(y, n)
+    convlv(data, respns, isign) -> array   src/Convolve.rs:8
+    correl(data1, data2) -> array          src/Correlation.rs:8
+    magnitude_spectrum / power_spectrum    src/FFT_1.rs:206,218
+
+Arrays are float64: numpy arrays (host memory; copied to and from the GPU
+inside the call) or torch CUDA tensors (device memory; no copies).  In-place
+routines modify their argument.  Every call runs on the GPU; there is no CPU
+path.  ``form`` selects the arithmetic: "fp64" (default, the crate's),
+"fp32", or "df64" (double-float pairs, FP64-class accuracy).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import FORMS
+
+__all__ = [
+    "four1", "four1_optimized", "FFTProcessor", "twofft", "realft", "fourn", "rlft3",
+    "cosft1", "cosft2", "sinft", "convlv", "correl", "convlv_batch", "correl_batch",
+    "autocorrel", "magnitude_spectrum", "power_spectrum", "real_to_complex",
+    "complex_to_real", "ConvlvError", "CorrelError", "GbfftError", "launch_count",
+]
+
+
+class GbfftError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("gbfft status %d: %s" % (status, msg))
+        self.status = status
+
+
+class ConvlvError(Exception):
+    """Mirror of ``ConvlvError`` (src/Convolve.rs:226-238)."""
+
+    class EmptyInput(Exception):
+        pass
+
+    class ResponseTooLong(Exception):
+        pass
+
+    class InvalidIsign(Exception):
+        pass
+
+
+class CorrelError(Exception):
+    """Mirror of ``CorrelError`` (src/Correlation.rs:389-399)."""
+
+    class EmptyInput(Exception):
+        pass
+
+    class LengthMismatch(Exception):
+        pass
+
+    class ZeroStdDev(Exception):
+        pass
+
+
+def _check(status):
+    if status != _lib.OK:
+        raise GbfftError(status, _lib.last_error())
+
+
+# ---------------------------------------------------------------------------
+# argument marshalling
+# ---------------------------------------------------------------------------
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+class _Arg:
+    """A float64 buffer as (pointer, number of doubles, on-device flag)."""
+
+    def __init__(self, a, writable):
+        if _is_torch(a):
+            import torch
+            if a.dtype != torch.float64:
+                raise TypeError("expected a float64 tensor")
+            if not a.is_contiguous():
+                raise ValueError("tensor must be contiguous")
+            self.dev = a.is_cuda
+            if not self.dev:
+                a = a.numpy()
+            else:
+                self.ptr = a.data_ptr()
+                self.size = a.numel()
+                self.obj = a
+                return
+        if not isinstance(a, np.ndarray):
+            if writable:
+                raise TypeError("in-place routines need a float64 numpy array or tensor")
+            a = np.ascontiguousarray(a, dtype=np.float64)
+        if a.dtype != np.float64:
+            if writable:
+                raise TypeError("expected a float64 array")
+            a = a.astype(np.float64)
+        if not a.flags.c_contiguous:
+            if writable:
+                raise ValueError("array must be C-contiguous")
+            a = np.ascontiguousarray(a)
+        if writable and not a.flags.writeable:
+            raise ValueError("array is read-only")
+        self.dev = False
+        self.obj = a
+        self.size = a.size
+        self.ptr = a.ctypes.data if a.size else None
+
+
+_ASYNC = [False]
+
+
+def set_async(flag):
+    """Device-tensor calls return without synchronising when set (work is
+    ordered on the current torch stream).  Host-array calls always wait."""
+    _ASYNC[0] = bool(flag)
+
+
+def _opts(args, form, stream=None):
+    devs = {a.dev for a in args}
+    if len(devs) > 1:
+        raise ValueError("mixing host arrays and device tensors in one call")
+    o = _lib.Opts()
+    o.form = FORMS[form] if isinstance(form, str) else int(form)
+    o.device_ptrs = 1 if devs == {True} else 0
+    o.stream = stream
+    o.async_ = 1 if (o.device_ptrs and _ASYNC[0]) else 0
+    if o.device_ptrs and stream is None:
+        import torch
+        o.stream = torch.cuda.current_stream().cuda_stream
+    return o
+
+
+def _new_like(proto, n):
+    if proto.dev:
+        import torch
+        return torch.empty(n, dtype=torch.float64, device=proto.obj.device)
+    return np.empty(n, dtype=np.float64)
+
+
+# ---------------------------------------------------------------------------
+# complex FFT
+# ---------------------------------------------------------------------------
+def four1(data, nn, isign, form="fp64"):
+    """In-place complex FFT of nn points (``src/FFT_1.rs:5``).
+
+    ``data`` holds 2*nn interleaved doubles.  isign=+1 uses exp(+2 pi i jk/N).
+    """
+    a = _Arg(data, True)
+    if a.size < 2 * nn:
+        raise ValueError("data holds %d doubles, need 2*nn=%d" % (a.size, 2 * nn))
+    o = _opts([a], form)
+    _check(_lib.load().gbfft_four1(a.ptr, nn, isign, ctypes.byref(o)))
+
+
+def four1_optimized(data, nn, isign, form="fp64"):
+    """``src/FFT_1.rs:110`` -- same transform as four1 (twiddles are exact on the GPU)."""
+    four1(data, nn, isign, form)
+
+
+def four1_many(data, nn, count, isign, dist=None, form="fp64"):
+    """``count`` transforms of nn points, ``dist`` doubles apart (default 2*nn)."""
+    a = _Arg(data, True)
+    dist = 2 * nn if dist is None else dist
+    o = _opts([a], form)
+    _check(_lib.load().gbfft_four1_many(a.ptr, nn, count, dist, isign, ctypes.byref(o)))
+
+
+class FFTProcessor:
+    """Mirror of ``FFTProcessor`` (src/FFT_1.rs:143-190)."""
+
+    def __init__(self, form="fp64"):
+        self.max_threads = 0
+        self.use_optimized = True
+        self.form = form
+
+    def with_threads(self, threads):
+        self.max_threads = threads  # the reference stores and ignores it as well
+        return self
+
+    def with_optimized(self, use_optimized):
+        self.use_optimized = use_optimized
+        return self
+
+    def fft(self, data, isign):
+        n = data.size if isinstance(data, np.ndarray) else data.numel()
+        four1(data, n // 2, isign, self.form)
+
+    def fft_batch(self, batches, isign):
+        """All transforms in one library call; sizes may differ."""
+        if not batches:
+            return
+        args = [_Arg(b, True) for b in batches]
+        o = _opts(args, self.form)
+        n = len(args)
+        ptrs = (ctypes.c_void_p * n)(*[x.ptr for x in args])
+        nns = (ctypes.c_size_t * n)(*[x.size // 2 for x in args])
+        _check(_lib.load().gbfft_four1_batch(ptrs, nns, n, isign, ctypes.byref(o)))
+
+
+def twofft(data1, data2, fft1, fft2, form="fp64"):
+    """Spectra of two real arrays from one complex FFT (``src/FFT_2.rs:3``).
+
+    fft1 and fft2 have length 2n+2 (as asserted at src/FFT_2.rs:6-7).
+    """
+    a1, a2 = _Arg(data1, False), _Arg(data2, False)
+    n = a1.size
+    if a2.size != n:
+        raise ValueError("data2 length must equal data1 length")
+    f1, f2 = _Arg(fft1, True), _Arg(fft2, True)
+    if f1.size != 2 * n + 2 or f2.size != 2 * n + 2:
+        raise ValueError("fft1 and fft2 must have length 2*n + 2")
+    o = _opts([a1, a2, f1, f2], form)
+    _check(_lib.load().gbfft_twofft(a1.ptr, a2.ptr, f1.ptr, f2.ptr, n, ctypes.byref(o)))
+
+
+def realft(data, n, isign, form="fp64"):
+    """In-place real FFT of n reals (``src/Real_FT.rs:4``), packed output."""
+    if n % 2 != 0:
+        raise ValueError("n must be even")
+    a = _Arg(data, True)
+    if a.size < n:
+        raise ValueError("data length must be at least n")
+    o = _opts([a], form)
+    _check(_lib.load().gbfft_realft(a.ptr, n, isign, ctypes.byref(o)))
+
+
+def fourn(data, nn, ndim, isign, form="fp64"):
+    """In-place N-D complex FFT, row-major (``src/Fourn.rs:278`` contract).
+
+    Raises ValueError for the inputs ``validate_inputs`` rejects
+    (src/Fourn.rs:367-378).
+    """
+    a = _Arg(data, True)
+    nn = list(nn)
+    arr = (ctypes.c_size_t * max(len(nn), 1))(*nn)
+    o = _opts([a], form)
+    st = _lib.load().gbfft_fourn(a.ptr, arr, len(nn), ndim, isign, ctypes.byref(o))
+    if st == _lib.INVALID_ARG:
+        raise ValueError(_lib.last_error())
+    _check(st)
+
+
+def rlft3(data, speq, nn1, nn2, nn3, isign, form="fp64"):
+    """3-D real FFT (``src/Real_FT3.rs:8``); speq holds nn1 x 2*nn2 doubles."""
+    if isign not in (1, -1):
+        raise ValueError("isign must be 1 or -1")
+    a, s = _Arg(data, True), _Arg(speq, True)
+    if a.size != nn1 * nn2 * nn3:
+        raise ValueError("data dimensions mismatch")
+    if s.size != nn1 * 2 * nn2:
+        raise ValueError("speq dimensions mismatch")
+    o = _opts([a, s], form)
+    _check(_lib.load().gbfft_rlft3(a.ptr, s.ptr, nn1, nn2, nn3, isign, ctypes.byref(o)))
+
+
+def sinft(y, n, form="fp64"):
+    a = _Arg(y, True)
+    o = _opts([a], form)
+    _check(_lib.load().gbfft_sinft(a.ptr, n, ctypes.byref(o)))
+
+
+def cosft1(y, n, form="fp64"):
+    """``src/Cos_FT.rs:7``; y holds n+1 values (0-based)."""
+    a = _Arg(y, True)
+    o = _opts([a], form)
+    _check(_lib.load().gbfft_cosft1(a.ptr, n, ctypes.byref(o)))
+
+
+def cosft2(y, n, isign, form="fp64"):
+    """``src/Cos_FT2.rs:7``; y holds n values (0-based)."""
+    if isign not in (1, -1):
+        raise ValueError("Invalid isign value: %d. Must be 1 or -1" % isign)
+    a = _Arg(y, True)
+    o = _opts([a], form)
+    _check(_lib.load().gbfft_cosft2(a.ptr, n, isign, ctypes.byref(o)))
+
+
+# ---------------------------------------------------------------------------
+# spectral routines
+# ---------------------------------------------------------------------------
+def convlv(data, respns, isign, form="fp64", out=None):
+    """Convolution / deconvolution (``src/Convolve.rs:8``); returns n reals.
+
+    Raises ConvlvError.EmptyInput / ResponseTooLong / InvalidIsign in the
+    order the reference checks them.  ``out`` may supply the result array.
+    """
+    a, r = _Arg(data, False), _Arg(respns, False)
+    n, m = a.size, r.size
+    if out is None:
+        out = _new_like(a, n)
+    o_arg = _Arg(out, True) if n else a
+    o = _opts([a, r], form)
+    st = _lib.load().gbfft_convlv(a.ptr, n, r.ptr, m, isign, o_arg.ptr if n else None,
+                                  ctypes.byref(o))
+    if st == _lib.EMPTY_INPUT:
+        raise ConvlvError.EmptyInput(_lib.last_error())
+    if st == _lib.RESPONSE_TOO_LONG:
+        raise ConvlvError.ResponseTooLong(_lib.last_error())
+    if st == _lib.INVALID_ISIGN:
+        raise ConvlvError.InvalidIsign(_lib.last_error())
+    _check(st)
+    return out
+
+
+def correl(data1, data2, form="fp64", out=None):
+    """Correlation (``src/Correlation.rs:8``); returns n reals."""
+    a, b = _Arg(data1, False), _Arg(data2, False)
+    n = a.size
+    if out is None:
+        out = _new_like(a, max(n, 1))
+    o_arg = _Arg(out, True)
+    o = _opts([a, b], form)
+    st = _lib.load().gbfft_correl(a.ptr, n, b.ptr, b.size, o_arg.ptr, ctypes.byref(o))
+    if st == _lib.EMPTY_INPUT:
+        raise CorrelError.EmptyInput(_lib.last_error())
+    if st == _lib.LENGTH_MISMATCH:
+        raise CorrelError.LengthMismatch(_lib.last_error())
+    _check(st)
+    return out[:n]
+
+
+def convlv_batch(data_batch, respns, isign, form="fp64"):
+    """``convlv_batch`` (src/Convolve.rs:241)."""
+    return [convlv(d, respns, isign, form) for d in data_batch]
+
+
+def correl_batch(pairs, form="fp64"):
+    """``correl_batch`` (src/Correlation.rs:273)."""
+    return [correl(a, b, form) for a, b in pairs]
+
+
+def autocorrel(data, form="fp64"):
+    """``autocorrel`` (src/Correlation.rs:281)."""
+    return correl(data, data, form)
+
+
+def magnitude_spectrum(c, form="fp64"):
+    a = _Arg(c, False)
+    out = _new_like(a, a.size // 2)
+    o = _opts([a], form)
+    _check(_lib.load().gbfft_magnitude_spectrum(a.ptr, a.size // 2, _Arg(out, True).ptr,
+                                                ctypes.byref(o)))
+    return out
+
+
+def power_spectrum(c, form="fp64"):
+    a = _Arg(c, False)
+    out = _new_like(a, a.size // 2)
+    o = _opts([a], form)
+    _check(_lib.load().gbfft_power_spectrum(a.ptr, a.size // 2, _Arg(out, True).ptr,
+                                            ctypes.byref(o)))
+    return out
+
+
+def real_to_complex(x):
+    """``src/FFT_1.rs:193``: interleave with zero imaginary parts (host helper)."""
+    x = np.asarray(x, dtype=np.float64)
+    out = np.zeros(2 * x.size)
+    out[0::2] = x
+    return out
+
+
+def complex_to_real(c):
+    """``src/FFT_1.rs:202``: the real parts (host helper)."""
+    return np.asarray(c, dtype=np.float64)[0::2].copy()
+
+
+def launch_count(reset=False):
+    """Kernel launches issued by the library since the last reset."""
+    return _lib.load().gbfft_launch_count(1 if reset else 0)
+
+
+PROFILE_KINDS = {"pass": 0, "twist": 1, "spectral": 2, "other": 3}
+
+
+def profile(enable):
+    """Start (and clear) or stop event timing of every library launch."""
+    _check(_lib.load().gbfft_profile(1 if enable else 0))
+
+
+def profile_read(kind):
+    """(total ms, launches, algorithmic bytes, nominal flops) of one kernel kind."""
+    ms = ctypes.c_double()
+    n = ctypes.c_longlong()
+    by = ctypes.c_double()
+    fl = ctypes.c_double()
+    _check(_lib.load().gbfft_profile_read(PROFILE_KINDS[kind], ctypes.byref(ms), ctypes.byref(n),
+                                          ctypes.byref(by), ctypes.byref(fl)))
+    return ms.value, n.value, by.value, fl.value

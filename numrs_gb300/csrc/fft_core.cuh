@@ -1,0 +1,344 @@
+// fft_core.cuh -- the Stockham pass kernel shared by every precision form.
+//
+// One launch performs one radix-R pass of a Stockham autosort FFT along an
+// axis (R <= 4096).  Each CTA loads a tile of C columns x R rows from global
+// memory (coalesced along whichever index is contiguous), multiplies by the
+// inter-pass twiddles, runs the R-point DFT of every column in shared memory
+// as a short sequence of radix-2/4/8/16 register sub-passes (themselves
+// Stockham steps), and stores the tile at the autosorted positions.  Axes of
+// at most 4096 points take one launch; longer axes take 2-3 launches that
+// ping-pong through one scratch buffer, the last one in place.
+#pragma once
+#include "arith.cuh"
+#include "gbfft_internal.h"
+
+namespace gbfft {
+
+constexpr int kEPT = 16;  // complex elements per thread per tile
+
+__device__ __forceinline__ int pidx(int i, int sh) { return i + (i >> sh); }
+
+// ---------------------------------------------------------------------------
+// Twiddle lookup: w_S^e with sign, S and e < S powers-of-two arithmetic.
+// ---------------------------------------------------------------------------
+template <class F>
+__device__ __forceinline__ typename F::C twiddle(const Twiddles& tw, int logS, long long e,
+                                                 int sg) {
+  using TW = typename F::TW;
+  const TW* dense = reinterpret_cast<const TW*>(tw.dense);
+  if (logS <= kDenseLog) return F::ld_tw(dense + ((1ll << logS) + e), sg);
+  const TW* part = reinterpret_cast<const TW*>(tw.partial);
+  typename F::C hi = F::ld_tw(dense + ((1ll << (logS - kPartialLog)) + (e >> kPartialLog)), sg);
+  typename F::C lo = F::ld_tw(part + ((long long)(logS - kDenseLog - 1) * kPartial +
+                                      (e & (kPartial - 1))), sg);
+  return F::mul(hi, lo);
+}
+
+// ---------------------------------------------------------------------------
+// Small DFTs in registers, X_k = sum_t v_t exp(+SG 2 pi i t k / Q), in place.
+// ---------------------------------------------------------------------------
+template <class F, int SG>
+__device__ __forceinline__ void dft2(typename F::C& a, typename F::C& b) {
+  typename F::C t = F::sub(a, b);
+  a = F::add(a, b);
+  b = t;
+}
+
+template <class F, int SG>
+__device__ __forceinline__ void dft4(typename F::C& a0, typename F::C& a1, typename F::C& a2,
+                                     typename F::C& a3) {
+  using C = typename F::C;
+  C t0 = F::add(a0, a2), t1 = F::sub(a0, a2);
+  C t2 = F::add(a1, a3), t3 = F::mul_j(F::sub(a1, a3), SG);
+  a0 = F::add(t0, t2);
+  a2 = F::sub(t0, t2);
+  a1 = F::add(t1, t3);
+  a3 = F::sub(t1, t3);
+}
+
+constexpr double kH = 0.70710678118654752440084436210484903928;   // cos(pi/4)
+constexpr double kC1 = 0.92387953251128675612818318939678828682;  // cos(pi/8)
+constexpr double kS1 = 0.38268343236508977172845998403039886676;  // sin(pi/8)
+
+template <class F, int SG>
+__device__ __forceinline__ void dft8(typename F::C* v) {
+  using C = typename F::C;
+  // decimation in time: even and odd 4-point DFTs, then twiddles w8^k
+  C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+  C o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+  dft4<F, SG>(e0, e1, e2, e3);
+  dft4<F, SG>(o0, o1, o2, o3);
+  o1 = F::rot45(o1, kH, SG);
+  o2 = F::mul_j(o2, SG);
+  o3 = F::mul_j(F::rot45(o3, kH, SG), SG);
+  v[0] = F::add(e0, o0); v[4] = F::sub(e0, o0);
+  v[1] = F::add(e1, o1); v[5] = F::sub(e1, o1);
+  v[2] = F::add(e2, o2); v[6] = F::sub(e2, o2);
+  v[3] = F::add(e3, o3); v[7] = F::sub(e3, o3);
+}
+
+template <class F, int SG>
+__device__ __forceinline__ void dft16(typename F::C* v) {
+  using C = typename F::C;
+  // 4 x 4: X_{k1+4k2} = sum_{n2} w4^{n2 k2} w16^{n2 k1} sum_{n1} v_{n2+4n1} w4^{n1 k1}
+  C a[4][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    a[n2][0] = v[n2]; a[n2][1] = v[n2 + 4]; a[n2][2] = v[n2 + 8]; a[n2][3] = v[n2 + 12];
+    dft4<F, SG>(a[n2][0], a[n2][1], a[n2][2], a[n2][3]);
+  }
+  // twiddles w16^{n2 k1}
+  a[1][1] = F::mulcs(a[1][1], kC1, SG * kS1);       // w^1
+  a[1][2] = F::rot45(a[1][2], kH, SG);              // w^2
+  a[1][3] = F::mulcs(a[1][3], kS1, SG * kC1);       // w^3
+  a[2][1] = F::rot45(a[2][1], kH, SG);              // w^2
+  a[2][2] = F::mul_j(a[2][2], SG);                  // w^4
+  a[2][3] = F::mul_j(F::rot45(a[2][3], kH, SG), SG);  // w^6
+  a[3][1] = F::mulcs(a[3][1], kS1, SG * kC1);       // w^3
+  a[3][2] = F::mul_j(F::rot45(a[3][2], kH, SG), SG);  // w^6
+  a[3][3] = F::mulcs(a[3][3], -kC1, -SG * kS1);     // w^9
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    C b0 = a[0][k1], b1 = a[1][k1], b2 = a[2][k1], b3 = a[3][k1];
+    dft4<F, SG>(b0, b1, b2, b3);
+    v[k1] = b0; v[k1 + 4] = b1; v[k1 + 8] = b2; v[k1 + 12] = b3;
+  }
+}
+
+template <class F, int SG, int Q>
+__device__ __forceinline__ void dftq(typename F::C* v) {
+  if constexpr (Q == 2) dft2<F, SG>(v[0], v[1]);
+  else if constexpr (Q == 4) dft4<F, SG>(v[0], v[1], v[2], v[3]);
+  else if constexpr (Q == 8) dft8<F, SG>(v);
+  else dft16<F, SG>(v);
+}
+
+// ---------------------------------------------------------------------------
+// One in-CTA Stockham sub-pass of radix Q over C columns of R points held in
+// shared memory (column c at c*R, padded).  Every thread owns 16/Q butterflies.
+// ---------------------------------------------------------------------------
+template <class F, int SG, int Q>
+__device__ __forceinline__ void subpass(typename F::S* sm, int logR, int logNs, const Twiddles& tw,
+                                        int tid, int T) {
+  using C = typename F::C;
+  constexpr int B = kEPT / Q;
+  constexpr int LQ = (Q == 2) ? 1 : (Q == 4) ? 2 : (Q == 8) ? 3 : 4;
+  constexpr int sh = F::kPadShift;
+  const int logRQ = logR - LQ;
+  const int RQ = 1 << logRQ;
+  const int Ns = 1 << logNs;
+  C v[B][Q];
+  int ob[B];
+#pragma unroll
+  for (int i = 0; i < B; ++i) {
+    const int b = tid + i * T;
+    const int c = b >> logRQ;
+    const int j = b & (RQ - 1);
+    const int base = c << logR;
+#pragma unroll
+    for (int t = 0; t < Q; ++t) v[i][t] = F::from_s(sm[pidx(base + j + t * RQ, sh)]);
+    const int jm = j & (Ns - 1);
+    if (logNs > 0 && jm != 0) {
+#pragma unroll
+      for (int t = 1; t < Q; ++t)
+        v[i][t] = F::mul(v[i][t], twiddle<F>(tw, logNs + LQ, (long long)jm * t, SG));
+    }
+    dftq<F, SG, Q>(v[i]);
+    ob[i] = base + ((j >> logNs) << (logNs + LQ)) + jm;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < B; ++i) {
+#pragma unroll
+    for (int t = 0; t < Q; ++t) sm[pidx(ob[i] + t * Ns, sh)] = F::to_s(v[i][t]);
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Global element access with format conversion.
+// ---------------------------------------------------------------------------
+template <class F, int IO>
+__device__ __forceinline__ typename F::C gload(const void* p, long long i) {
+  if constexpr (IO == IO_D2) {
+    d2 v = reinterpret_cast<const d2*>(p)[i];
+    return F::from_d(v.x, v.y);
+  } else if constexpr (IO == IO_F2) {
+    f2 v = reinterpret_cast<const f2*>(p)[i];
+    if constexpr (F::kind == 1) {
+      return F::from_s(v);
+    } else {
+      return F::from_d((double)v.x, (double)v.y);
+    }
+  } else {
+    f4 v = reinterpret_cast<const f4*>(p)[i];
+    if constexpr (F::kind == 2) {
+      return F::from_s(v);
+    } else {
+      return F::from_d((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+    }
+  }
+}
+
+template <class F, int IO>
+__device__ __forceinline__ void gstore(void* p, long long i, typename F::C a) {
+  if constexpr (IO == IO_D2) {
+    double x, y;
+    F::to_d(a, x, y);
+    reinterpret_cast<d2*>(p)[i] = d2{x, y};
+  } else if constexpr (IO == IO_F2) {
+    if constexpr (F::kind == 1) {
+      reinterpret_cast<f2*>(p)[i] = F::to_s(a);
+    } else {
+      double x, y;
+      F::to_d(a, x, y);
+      reinterpret_cast<f2*>(p)[i] = f2{(float)x, (float)y};
+    }
+  } else {
+    if constexpr (F::kind == 2) {
+      reinterpret_cast<f4*>(p)[i] = F::to_s(a);
+    } else {
+      double x, y;
+      F::to_d(a, x, y);
+      float xh = (float)x, yh = (float)y;
+      reinterpret_cast<f4*>(p)[i] = f4{xh, (float)(x - xh), yh, (float)(y - yh)};
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The pass kernel.  T threads, tile of 16*T complex elements.
+// ---------------------------------------------------------------------------
+template <class F, int SG, int IN, int OUT, int T>
+__global__ void __launch_bounds__(T) k_pass(PassParams p) {
+  using C = typename F::C;
+  using S = typename F::S;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  S* sm = reinterpret_cast<S*>(smem_raw);
+  constexpr int sh = F::kPadShift;
+  const int tid = threadIdx.x;
+  const int logR = p.logR, logC = p.logC;
+  const int R = 1 << logR;
+  const int Cn = 1 << logC;
+  const long long tile = blockIdx.x;
+
+  // tile -> (first line, first j)
+  long long line0, j0;
+  const int logLR = p.logL - logR;  // log2(L/R)
+  if (p.mode == 0) {
+    const int logTpl = logLR - logC;  // tiles per line
+    line0 = tile >> logTpl;
+    j0 = (tile & ((1ll << logTpl) - 1)) << logC;
+  } else {
+    const long long ng = (p.nlines + Cn - 1) >> logC;
+    j0 = tile / ng;
+    line0 = (tile - j0 * ng) << logC;
+  }
+  const long long lqmask = (1ll << p.lq_log) - 1;
+
+  // ---- load tile: global -> (twiddle) -> shared ----
+#pragma unroll 4
+  for (int k = 0; k < kEPT; ++k) {
+    const int e = tid + k * T;
+    int c, r;
+    if (p.in_rcontig) { r = e & (R - 1); c = e >> logR; }
+    else { c = e & (Cn - 1); r = e >> logC; }
+    long long line = line0, j = j0;
+    if (p.mode == 0) j += c; else line += c;
+    C v;
+    if (line < p.nlines) {
+      const long long base = (line >> p.lq_log) * p.lstride + (line & lqmask);
+      const long long idx = base + (j + ((long long)r << logLR)) * p.s;
+      v = gload<F, IN>(p.in, idx);
+      if (p.logNs > 0) {
+        const long long jm = j & (p.Ns - 1);
+        if (jm != 0 && r != 0) v = F::mul(v, twiddle<F>(p.tw, p.logNs + logR, jm * r, SG));
+      }
+    } else {
+      v = F::from_d(0.0, 0.0);
+    }
+    sm[pidx((c << logR) + r, sh)] = F::to_s(v);
+  }
+  __syncthreads();
+
+  // ---- R-point DFTs of the C columns ----
+  int logNsub = 0;
+  for (int k = 0; k < p.nq; ++k) {
+    const int lq = p.q[k];
+    switch (lq) {
+      case 4: subpass<F, SG, 16>(sm, logR, logNsub, p.tw, tid, T); break;
+      case 3: subpass<F, SG, 8>(sm, logR, logNsub, p.tw, tid, T); break;
+      case 2: subpass<F, SG, 4>(sm, logR, logNsub, p.tw, tid, T); break;
+      default: subpass<F, SG, 2>(sm, logR, logNsub, p.tw, tid, T); break;
+    }
+    logNsub += lq;
+  }
+
+  // ---- store tile: shared -> global at the autosorted positions ----
+#pragma unroll 4
+  for (int k = 0; k < kEPT; ++k) {
+    const int e = tid + k * T;
+    int c, r;
+    if (p.out_rcontig) { r = e & (R - 1); c = e >> logR; }
+    else { c = e & (Cn - 1); r = e >> logC; }
+    long long line = line0, j = j0;
+    if (p.mode == 0) j += c; else line += c;
+    if (line >= p.nlines) continue;
+    C v = F::from_s(sm[pidx((c << logR) + r, sh)]);
+    if (p.do_scale) v = F::scale(v, p.scale);
+    const long long base = (line >> p.lq_log) * p.lstride + (line & lqmask);
+    const long long jd = ((j >> p.logNs) << (p.logNs + logR)) + (j & (p.Ns - 1));
+    const long long idx = base + (jd + ((long long)r << p.logNs)) * p.s;
+    gstore<F, OUT>(p.out, idx, v);
+  }
+}
+
+template <class F>
+inline size_t pass_smem_bytes(int T) {
+  const int E = kEPT * T;
+  return sizeof(typename F::S) * (size_t)(E + (E >> F::kPadShift));
+}
+
+template <class K>
+inline void set_smem_once(K k, size_t smem) {
+  static size_t done = 0;  // one static per kernel instantiation
+  if (done < smem) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    done = smem;
+  }
+}
+
+template <class F, int SG, int IN, int OUT>
+cudaError_t launch_pass_t(const PassParams& p, int threads, cudaStream_t st) {
+  const size_t smem = pass_smem_bytes<F>(threads);
+  dim3 grid((unsigned)p.tiles);
+  switch (threads) {
+    case 256: {
+      auto k = k_pass<F, SG, IN, OUT, 256>;
+      set_smem_once(k, smem);
+      k<<<grid, 256, smem, st>>>(p);
+      break;
+    }
+    case 128: {
+      auto k = k_pass<F, SG, IN, OUT, 128>;
+      set_smem_once(k, smem);
+      k<<<grid, 128, smem, st>>>(p);
+      break;
+    }
+    case 64: {
+      auto k = k_pass<F, SG, IN, OUT, 64>;
+      set_smem_once(k, smem);
+      k<<<grid, 64, smem, st>>>(p);
+      break;
+    }
+    default: {
+      auto k = k_pass<F, SG, IN, OUT, 32>;
+      set_smem_once(k, smem);
+      k<<<grid, 32, smem, st>>>(p);
+      break;
+    }
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace gbfft

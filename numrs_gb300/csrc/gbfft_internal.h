@@ -1,0 +1,125 @@
+// gbfft_internal.h -- declarations shared by the kernel translation units and
+// the host runtime.  Nothing here is part of the public C ABI (include/gbfft.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+
+namespace gbfft {
+
+enum Form : int { FORM_F64 = 0, FORM_F32 = 1, FORM_DF64 = 2 };
+
+// Element types a pass reads or writes in global memory.
+//   IO_D2  interleaved double complex (the caller's layout)
+//   IO_F2  float complex (FP32 intermediate)
+//   IO_F4  double-float complex (re.hi, re.lo, im.hi, im.lo) (DF64 intermediate)
+enum IOType : int { IO_D2 = 0, IO_F2 = 1, IO_F4 = 2 };
+
+inline size_t io_bytes(IOType t) { return t == IO_F2 ? 8 : 16; }
+
+// Twiddle tables of one form.  dense holds levels S = 2^1 .. 2^kDenseLog
+// back to back, entry S+e = exp(+2 pi i e / S).  partial holds, for each
+// level S = 2^(kDenseLog+1) .. 2^kMaxLog, the first kPartial entries of that
+// level; a twiddle of a larger level is the product of one dense entry of
+// level S/kPartial and one partial entry.
+constexpr int kDenseLog = 16;
+constexpr int kPartialLog = 12;
+constexpr int kPartial = 1 << kPartialLog;
+constexpr int kMaxLog = kDenseLog + kPartialLog;  // 2^28 points per axis
+constexpr size_t kDenseEntries = size_t(2) << kDenseLog;
+constexpr size_t kPartialEntries = size_t(kMaxLog - kDenseLog) * kPartial;
+
+struct Twiddles {
+  const void* dense = nullptr;
+  const void* partial = nullptr;
+};
+
+// One Stockham pass over an axis.  The axis has length L and stride s
+// (complex elements).  Lines are the independent 1-D sequences along the
+// axis; line l starts at (l >> lq_log) * lstride + (l & ((1<<lq_log)-1)).
+// The pass applies, to every column j in [0, L/R), the twiddles
+// w_{Ns R}^{(j mod Ns) r} and an R-point DFT, reading element r at
+// j + r L/R and writing it at expand(j) + r Ns (Stockham autosort).
+// A CTA works on a tile of C = 2^logC columns:
+//   mode 0  the columns are C consecutive j of one line (s == 1, L/R >= C)
+//   mode 1  the columns are C consecutive lines at one j
+struct PassParams {
+  const void* in;
+  void* out;
+  Twiddles tw;
+  long long L;
+  long long s;
+  long long lstride;
+  long long nlines;
+  long long Ns;
+  int lq_log;
+  int logL;
+  int logR;
+  int logC;
+  int logNs;
+  int mode;
+  int in_rcontig;   // 1: tile elements are contiguous along r in global memory
+  int out_rcontig;
+  int nq;
+  int q[4];         // log2 of the in-CTA sub-pass radices (sum = logR)
+  int do_scale;
+  double scale;
+  long long tiles;  // grid size
+};
+
+// kernel launchers (one per form, defined in fft_<form>.cu)
+cudaError_t launch_pass_f64(int sign, IOType in, IOType out, const PassParams& p, int threads,
+                            cudaStream_t st);
+cudaError_t launch_pass_f32(int sign, IOType in, IOType out, const PassParams& p, int threads,
+                            cudaStream_t st);
+cudaError_t launch_pass_df64(int sign, IOType in, IOType out, const PassParams& p, int threads,
+                             cudaStream_t st);
+cudaError_t launch_twiddles(Form f, void* dense, void* partial, cudaStream_t st);
+
+// spectral / real-transform kernels (spectral.cu)
+struct SpecArgs {
+  Twiddles tw;
+  int form;
+};
+// realft twist on `batch` packed real transforms of n reals each (data viewed
+// as n/2 complex), lines `dist` doubles apart.  isign=+1: after the forward
+// n/2-point FFT; isign=-1: before the inverse FFT.
+cudaError_t launch_realft_twist(Form f, int isign, double* data, long long n, long long batch,
+                                long long dist, Twiddles tw, cudaStream_t st);
+// Fused convlv/correl spectral step on two raw n/2-point spectra A (data) and
+// B (response / data2), each n/2 complex: forward twists, product (kind 0:
+// convolve, 1: deconvolve, 2: correlate), scale 1/(n/2), inverse twist.
+// Writes the packed input of the inverse n/2-point FFT to out (may alias a).
+cudaError_t launch_spectral_product(Form f, int kind, const double* a, const double* b,
+                                    double* out, long long n, Twiddles tw, cudaStream_t st);
+// Numerical Recipes wrap-around expansion of an m-tap response into n reals;
+// also copies `data` (n reals) to dst_data when non-null.
+cudaError_t launch_expand_response(const double* respns, long long m, double* dst, long long n,
+                                   const double* data, double* dst_data, cudaStream_t st);
+// Direct linear correlation for n <= 32 (the reference's small-n branch).
+cudaError_t launch_correl_direct(const double* a, const double* b, double* out, long long n,
+                                 cudaStream_t st);
+// twofft split (Numerical Recipes contract): fft1 holds the n-point FFT of
+// data1 + i data2; writes the two spectra into fft1 / fft2.
+cudaError_t launch_twofft_pack(const double* d1, const double* d2, double* fft1, long long n,
+                               cudaStream_t st);
+cudaError_t launch_twofft_split(double* fft1, double* fft2, long long n, cudaStream_t st);
+// rlft3 steps: speq gather (forward) and the twist along the last axis.
+cudaError_t launch_rlft3_speq(const double* data, double* speq, long long nn1, long long nn2,
+                              long long nn3, cudaStream_t st);
+cudaError_t launch_rlft3_twist(Form f, int isign, double* data, double* speq, long long nn1,
+                               long long nn2, long long nn3, Twiddles tw, cudaStream_t st);
+// sine / cosine transform pre- and post-passes around realft.
+cudaError_t launch_sinft_pre(double* y, long long n, Twiddles tw, cudaStream_t st);
+cudaError_t launch_cosft1_pre(double* y, long long n, double* partial, Twiddles tw,
+                              cudaStream_t st);
+cudaError_t launch_cosft2_pre(int isign, double* y, long long n, Twiddles tw, cudaStream_t st);
+cudaError_t launch_cosft2_rot(int isign, double* y, long long n, Twiddles tw, cudaStream_t st);
+// Ordered prefix sums on the odd/even slots after realft (sinft/cosft1/cosft2).
+cudaError_t launch_trig_scan(int kind, double* y, long long n, double* partial, double* work,
+                             cudaStream_t st);
+cudaError_t launch_scale(double* data, long long count, double s, cudaStream_t st);
+cudaError_t launch_spectrum(int kind, const double* c, double* out, long long nn,
+                            cudaStream_t st);
+
+}  // namespace gbfft

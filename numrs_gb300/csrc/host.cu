@@ -1,0 +1,891 @@
+// host.cu -- runtime behind the C ABI: device context, twiddle tables,
+// axis plans (Stockham pass schedules), scratch management and the entry
+// points declared in include/gbfft.h.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/gbfft.h"
+#include "gbfft_internal.h"
+
+namespace gbfft {
+
+namespace {
+
+constexpr int kTileE = 4096;     // complex elements per CTA tile
+constexpr int kMaxPassLog = 10;  // radix of a pass in a multi-pass schedule
+constexpr int kMaxAxisLog = kMaxLog;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct ProfRec {
+  int kind;
+  cudaEvent_t a, b;
+  double bytes;
+  double flops;
+};
+
+struct Ctx {
+  bool inited = false;
+  int device = 0;
+  cudaStream_t stream = nullptr;  // library stream
+  cudaStream_t cur = nullptr;     // stream of the call in progress
+  void* tw_dense[3] = {nullptr, nullptr, nullptr};
+  void* tw_part[3] = {nullptr, nullptr, nullptr};
+  DevBuf scratch;   // Stockham ping-pong buffer
+  DevBuf work;      // spectral working set (two n-real lines)
+  DevBuf stage_a;   // device copies of host arguments
+  DevBuf stage_b;
+  DevBuf stage_c;
+  DevBuf ptrtab;
+  std::vector<char> host_pack;
+  std::string err;
+  long long launches = 0;
+  bool profiling = false;
+  std::vector<ProfRec> prof;
+  std::vector<cudaEvent_t> evpool;
+};
+
+Ctx g;
+std::mutex g_mu;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g.err = buf;
+  return code;
+}
+
+#define CK(call)                                                                           \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(e_ == cudaErrorMemoryAllocation ? GBFFT_OOM : GBFFT_CUDA_ERROR,          \
+                  "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);    \
+  } while (0)
+
+#define TRY(expr)            \
+  do {                       \
+    int s_ = (expr);         \
+    if (s_ != GBFFT_OK) return s_; \
+  } while (0)
+
+bool is_pow2(unsigned long long x) { return x && !(x & (x - 1)); }
+int ilog2(unsigned long long x) { return 63 - __builtin_clzll(x); }
+unsigned long long npow2(unsigned long long x) {
+  unsigned long long p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+int ensure(DevBuf& b, size_t bytes) {
+  if (b.bytes >= bytes) return GBFFT_OK;
+  if (b.p) {
+    cudaDeviceSynchronize();
+    cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+  }
+  size_t want = std::max(bytes, (size_t)1 << 20);
+  cudaError_t e = cudaMalloc(&b.p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(GBFFT_OOM, "cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
+  }
+  b.bytes = want;
+  return GBFFT_OK;
+}
+
+int init_locked(int device) {
+  if (g.inited) return GBFFT_OK;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    return fail(GBFFT_CUDA_ERROR, "no CUDA device: %s", cudaGetErrorString(e));
+  CK(cudaSetDevice(device));
+  CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+  g.cur = g.stream;
+  g.device = device;
+  g.inited = true;
+  return GBFFT_OK;
+}
+
+int tables(Form f, Twiddles& tw) {
+  if (!g.tw_dense[f]) {
+    size_t esz = (f == FORM_F32) ? 8 : 16;
+    CK(cudaMalloc(&g.tw_dense[f], kDenseEntries * esz));
+    CK(cudaMalloc(&g.tw_part[f], kPartialEntries * esz));
+    CK(launch_twiddles(f, g.tw_dense[f], g.tw_part[f], g.cur));
+    g.launches++;
+  }
+  tw.dense = g.tw_dense[f];
+  tw.partial = g.tw_part[f];
+  return GBFFT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Optional per-kernel timing: events around every launch on the launching
+// stream, summed per kernel kind on request.
+// ---------------------------------------------------------------------------
+enum ProfKind { PK_PASS = 0, PK_TWIST = 1, PK_SPECTRAL = 2, PK_OTHER = 3, PK_COUNT = 4 };
+
+cudaEvent_t pool_event() {
+  if (!g.evpool.empty()) {
+    cudaEvent_t e = g.evpool.back();
+    g.evpool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+struct ProfScope {
+  bool on;
+  ProfRec r;
+  ProfScope(int kind, double bytes, double flops = 0.0) : on(g.profiling) {
+    if (!on) return;
+    r.kind = kind;
+    r.bytes = bytes;
+    r.flops = flops;
+    r.a = pool_event();
+    r.b = pool_event();
+    cudaEventRecord(r.a, g.cur);
+  }
+  ~ProfScope() {
+    if (!on) return;
+    cudaEventRecord(r.b, g.cur);
+    g.prof.push_back(r);
+  }
+};
+
+IOType scratch_io(Form f) { return f == FORM_F64 ? IO_D2 : (f == FORM_F32 ? IO_F2 : IO_F4); }
+
+// ---------------------------------------------------------------------------
+// Axis plan: the Stockham pass schedule for `nlines` lines of length L along
+// an axis of stride s.  Line l starts at (l >> lq_log) * lstride + (l & mask).
+// ---------------------------------------------------------------------------
+struct Pass {
+  PassParams p;
+  int threads;
+  int in_user;   // 1: reads the caller buffer, 0: the scratch buffer
+  int out_user;
+};
+
+struct AxisPlan {
+  std::vector<Pass> passes;
+  size_t scratch_elems = 0;
+};
+
+void split_subpasses(int logR, PassParams& p) {
+  int nsub = (logR + 3) / 4;
+  if (nsub < 1) nsub = 1;
+  int base = logR / nsub, extra = logR % nsub;
+  p.nq = nsub;
+  for (int i = 0; i < 4; ++i) p.q[i] = 0;
+  for (int i = 0; i < nsub; ++i) p.q[i] = base + (i < extra ? 1 : 0);
+}
+
+AxisPlan make_axis_plan(long long L, long long s, long long nlines, int lq_log,
+                        long long lstride) {
+  AxisPlan ap;
+  const int logL = ilog2((unsigned long long)L);
+  std::vector<int> radix;
+  if (logL <= 12) {
+    radix.push_back(logL);
+  } else {
+    int P = (logL + kMaxPassLog - 1) / kMaxPassLog;
+    int base = logL / P, extra = logL % P;
+    for (int i = 0; i < P; ++i) radix.push_back(base + (i < extra ? 1 : 0));
+  }
+  int logNs = 0;
+  const int P = (int)radix.size();
+  for (int i = 0; i < P; ++i) {
+    Pass ps;
+    PassParams& p = ps.p;
+    std::memset(&p, 0, sizeof p);
+    const int logR = radix[i];
+    p.L = L;
+    p.s = s;
+    p.lstride = lstride;
+    p.nlines = nlines;
+    p.lq_log = lq_log;
+    p.logL = logL;
+    p.logR = logR;
+    p.logNs = logNs;
+    p.Ns = 1ll << logNs;
+    const long long LR = L >> logR;
+    int logC;
+    if (s == 1 && LR > 1) {
+      p.mode = 0;
+      logC = std::min(ilog2(kTileE) - logR, ilog2((unsigned long long)LR));
+      p.in_rcontig = 0;
+      p.out_rcontig = (logNs == 0) ? 1 : 0;
+    } else {
+      p.mode = 1;
+      int want = ilog2(kTileE) - logR;
+      int have = ilog2(npow2((unsigned long long)nlines));
+      logC = std::min(want, have);
+      p.in_rcontig = (s == 1) ? 1 : 0;
+      p.out_rcontig = (s == 1) ? 1 : 0;
+    }
+    // at least one full warp: 16 * 32 = 512 elements per tile
+    if (logR + logC < 9) logC = 9 - logR;
+    p.logC = logC;
+    ps.threads = (1 << (logR + logC)) / 16;
+    split_subpasses(logR, p);
+    if (p.mode == 0) p.tiles = nlines * (LR >> logC);
+    else p.tiles = LR * ((nlines + (1ll << logC) - 1) >> logC);
+    p.do_scale = 0;
+    p.scale = 1.0;
+    ap.passes.push_back(ps);
+    logNs += logR;
+  }
+  // buffers: ping-pong through scratch, last pass into the caller buffer
+  bool in_user = true;
+  for (int i = 0; i < P; ++i) {
+    Pass& ps = ap.passes[i];
+    ps.in_user = in_user ? 1 : 0;
+    if (i == P - 1) ps.out_user = 1;
+    else ps.out_user = in_user ? 0 : 1;
+    in_user = ps.out_user;
+  }
+  if (P > 1) {
+    // the scratch mirrors the caller layout
+    if (s == 1) ap.scratch_elems = (size_t)((nlines - 1) * lstride + L);
+    else ap.scratch_elems = (size_t)(nlines * L);
+  }
+  return ap;
+}
+
+int launch_pass(Form f, int sign, IOType in, IOType out, const PassParams& p, int threads) {
+  cudaError_t e;
+  const double pts = (double)p.L * (double)p.nlines;
+  ProfScope ps(PK_PASS, pts * (double)(io_bytes(in) + io_bytes(out)), 5.0 * pts * p.logR);
+  if (f == FORM_F64) e = launch_pass_f64(sign, in, out, p, threads, g.cur);
+  else if (f == FORM_F32) e = launch_pass_f32(sign, in, out, p, threads, g.cur);
+  else e = launch_pass_df64(sign, in, out, p, threads, g.cur);
+  g.launches++;
+  if (e != cudaSuccess)
+    return fail(GBFFT_CUDA_ERROR, "pass launch (L=%lld R=2^%d): %s", p.L, p.logR,
+                cudaGetErrorString(e));
+  return GBFFT_OK;
+}
+
+// Run an axis plan on `data` (interleaved double complex, device memory).
+int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale = 1.0) {
+  Twiddles tw;
+  TRY(tables(f, tw));
+  const IOType sio = scratch_io(f);
+  if (ap.scratch_elems) TRY(ensure(g.scratch, ap.scratch_elems * io_bytes(sio)));
+  for (size_t i = 0; i < ap.passes.size(); ++i) {
+    const Pass& ps = ap.passes[i];
+    PassParams p = ps.p;
+    p.tw = tw;
+    p.in = ps.in_user ? data : g.scratch.p;
+    p.out = ps.out_user ? data : g.scratch.p;
+    if (i + 1 == ap.passes.size() && scale != 1.0) {
+      p.do_scale = 1;
+      p.scale = scale;
+    }
+    TRY(launch_pass(f, sign, ps.in_user ? IO_D2 : sio, ps.out_user ? IO_D2 : sio, p, ps.threads));
+  }
+  return GBFFT_OK;
+}
+
+// Plan cache keyed by (L, s, nlines, lq_log, lstride).
+std::map<std::tuple<long long, long long, long long, int, long long>, AxisPlan> g_plans;
+
+const AxisPlan& axis_plan(long long L, long long s, long long nlines, int lq_log,
+                          long long lstride) {
+  auto key = std::make_tuple(L, s, nlines, lq_log, lstride);
+  auto it = g_plans.find(key);
+  if (it != g_plans.end()) return it->second;
+  return g_plans.emplace(key, make_axis_plan(L, s, nlines, lq_log, lstride)).first->second;
+}
+
+// Contiguous batch of 1-D complex transforms: nlines lines `dist` complex apart.
+int fft_lines(Form f, int sign, void* data, long long L, long long nlines, long long dist,
+              double scale = 1.0) {
+  if (L == 1) {
+    if (scale != 1.0) {
+      // scaling of a 1-point transform: every line holds one complex value
+      for (long long l = 0; l < nlines; ++l) {
+        CK(launch_scale((double*)data + 2 * l * dist, 2, scale, g.cur));
+        g.launches++;
+      }
+    }
+    return GBFFT_OK;
+  }
+  return run_axis(f, sign, axis_plan(L, 1, nlines, 0, dist), data, scale);
+}
+
+struct Call {
+  const gbfft_opts* o;
+  gbfft_opts def;
+  explicit Call(const gbfft_opts* opts) {
+    std::memset(&def, 0, sizeof def);
+    o = opts ? opts : &def;
+  }
+  Form form() const { return (Form)o->form; }
+  bool dev() const { return o->device_ptrs != 0; }
+};
+
+int check_form(const Call& c) {
+  if (c.o->form < 0 || c.o->form > 2) return fail(GBFFT_INVALID_ARG, "unknown form %d", c.o->form);
+  return GBFFT_OK;
+}
+
+// Stream handling: a device-pointer call that names a stream runs on it;
+// every other call runs on the library stream.
+struct StreamScope {
+  explicit StreamScope(const Call& c) {
+    g.cur = (c.dev() && c.o->stream) ? (cudaStream_t)c.o->stream : g.stream;
+  }
+  int finish(const Call& c) {
+    if (!c.dev() || !c.o->async) CK(cudaStreamSynchronize(g.cur));
+    CK(cudaGetLastError());
+    g.cur = g.stream;
+    return GBFFT_OK;
+  }
+};
+
+int h2d(void* dst, const void* src, size_t bytes) {
+  CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, g.cur));
+  return GBFFT_OK;
+}
+int d2h(void* dst, const void* src, size_t bytes) {
+  CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, g.cur));
+  return GBFFT_OK;
+}
+int d2d(void* dst, const void* src, size_t bytes) {
+  if (dst == src || bytes == 0) return GBFFT_OK;
+  CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, g.cur));
+  return GBFFT_OK;
+}
+
+// Device view of an in/out array: the caller's pointer, or a staged copy.
+int stage_inout(const Call& c, DevBuf& buf, double* user, size_t doubles, double** dptr,
+                bool copy_in = true) {
+  if (c.dev()) {
+    *dptr = user;
+    return GBFFT_OK;
+  }
+  TRY(ensure(buf, doubles * sizeof(double)));
+  *dptr = (double*)buf.p;
+  if (copy_in) TRY(h2d(buf.p, user, doubles * sizeof(double)));
+  return GBFFT_OK;
+}
+int unstage(const Call& c, double* user, const double* dptr, size_t doubles) {
+  if (c.dev()) return GBFFT_OK;
+  return d2h(user, dptr, doubles * sizeof(double));
+}
+
+int check_isign(int isign) {
+  if (isign != 1 && isign != -1) return fail(GBFFT_INVALID_ARG, "isign must be 1 or -1, got %d", isign);
+  return GBFFT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// realft on device data (n reals, power of two >= 2), `batch` lines `dist`
+// doubles apart.
+// ---------------------------------------------------------------------------
+int realft_dev(Form f, double* d, long long n, int isign, long long batch = 1,
+               long long dist = 0) {
+  if (dist == 0) dist = n;
+  Twiddles tw;
+  TRY(tables(f, tw));
+  const long long nh = n / 2;
+  if (isign == 1) {
+    TRY(fft_lines(f, 1, d, nh, batch, dist / 2));
+    {
+      ProfScope ps(PK_TWIST, 2.0 * n * batch * 8);
+      CK(launch_realft_twist(f, 1, d, n, batch, dist, tw, g.cur));
+    }
+    g.launches++;
+  } else {
+    {
+      ProfScope ps(PK_TWIST, 2.0 * n * batch * 8);
+      CK(launch_realft_twist(f, -1, d, n, batch, dist, tw, g.cur));
+    }
+    g.launches++;
+    TRY(fft_lines(f, -1, d, nh, batch, dist / 2));
+  }
+  return GBFFT_OK;
+}
+
+// fourn on device data
+int fourn_dev(Form f, double* d, const long long* nn, int ndim, int isign) {
+  long long total = 1;
+  for (int i = 0; i < ndim; ++i) total *= nn[i];
+  long long s = 1;
+  for (int dd = ndim - 1; dd >= 0; --dd) {
+    long long L = nn[dd];
+    if (L > 1) {
+      long long nl = total / L;
+      if (s == 1) {
+        TRY(run_axis(f, isign, axis_plan(L, 1, nl, 0, L), d));
+      } else {
+        TRY(run_axis(f, isign, axis_plan(L, s, nl, ilog2((unsigned long long)s), L * s), d));
+      }
+    }
+    s *= L;
+  }
+  return GBFFT_OK;
+}
+
+// Two real lines of n in `w` (2n doubles): forward FFT both, fused spectral
+// step into line 0, inverse FFT of line 0.
+int spectral_dev(Form f, int kind, double* w, long long n) {
+  Twiddles tw;
+  TRY(tables(f, tw));
+  const long long nh = n / 2;
+  TRY(fft_lines(f, 1, w, nh, 2, nh));
+  {
+    ProfScope ps(PK_SPECTRAL, 3.0 * n * 8);
+    CK(launch_spectral_product(f, kind, w, w + n, w, n, tw, g.cur));
+  }
+  g.launches++;
+  TRY(fft_lines(f, -1, w, nh, 1, nh));
+  return GBFFT_OK;
+}
+
+}  // namespace
+}  // namespace gbfft
+
+using namespace gbfft;
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int gbfft_init(int device) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return init_locked(device);
+}
+
+const char* gbfft_last_error(void) { return g.err.c_str(); }
+
+int gbfft_version(void) { return 100; }
+
+size_t gbfft_scratch_bytes(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return g.scratch.bytes + g.work.bytes + g.stage_a.bytes + g.stage_b.bytes + g.stage_c.bytes;
+}
+
+int gbfft_release(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.inited) return GBFFT_OK;
+  cudaDeviceSynchronize();
+  for (DevBuf* b : {&g.scratch, &g.work, &g.stage_a, &g.stage_b, &g.stage_c, &g.ptrtab}) {
+    if (b->p) cudaFree(b->p);
+    b->p = nullptr;
+    b->bytes = 0;
+  }
+  g_plans.clear();
+  return GBFFT_OK;
+}
+
+int gbfft_profile(int enable) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g.inited) cudaDeviceSynchronize();
+  for (auto& r : g.prof) {
+    g.evpool.push_back(r.a);
+    g.evpool.push_back(r.b);
+  }
+  g.prof.clear();
+  g.profiling = enable != 0;
+  return GBFFT_OK;
+}
+
+int gbfft_profile_read(int kind, double* ms, long long* launches, double* bytes,
+                       double* flops) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (kind < 0 || kind >= PK_COUNT) return fail(GBFFT_INVALID_ARG, "profile kind %d", kind);
+  double t = 0.0, by = 0.0, fl = 0.0;
+  long long n = 0;
+  for (auto& r : g.prof) {
+    if (r.kind != kind) continue;
+    CK(cudaEventSynchronize(r.b));
+    float x = 0.f;
+    CK(cudaEventElapsedTime(&x, r.a, r.b));
+    t += x;
+    by += r.bytes;
+    fl += r.flops;
+    ++n;
+  }
+  if (ms) *ms = t;
+  if (launches) *launches = n;
+  if (bytes) *bytes = by;
+  if (flops) *flops = fl;
+  return GBFFT_OK;
+}
+
+long long gbfft_launch_count(int reset) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  long long v = g.launches;
+  if (reset) g.launches = 0;
+  return v;
+}
+
+int gbfft_four1(double* data, size_t nn, int isign, const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  if (!data) return fail(GBFFT_INVALID_ARG, "four1: null data");
+  TRY(check_isign(isign));
+  if (!is_pow2(nn) || ilog2(nn) > kMaxAxisLog)
+    return fail(GBFFT_UNSUPPORTED_SIZE, "four1: nn=%zu must be a power of two <= 2^%d", nn, kMaxAxisLog);
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  double* d;
+  TRY(stage_inout(c, g.stage_a, data, 2 * nn, &d));
+  TRY(fft_lines(c.form(), isign, d, (long long)nn, 1, (long long)nn));
+  TRY(unstage(c, data, d, 2 * nn));
+  return ss.finish(c);
+}
+
+int gbfft_four1_many(double* data, size_t nn, size_t count, size_t dist, int isign,
+                     const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  if (!data && count) return fail(GBFFT_INVALID_ARG, "four1_many: null data");
+  TRY(check_isign(isign));
+  if (!is_pow2(nn) || ilog2(nn) > kMaxAxisLog)
+    return fail(GBFFT_UNSUPPORTED_SIZE, "four1_many: nn=%zu must be a power of two", nn);
+  if (dist < 2 * nn || (dist & 1)) return fail(GBFFT_INVALID_ARG, "four1_many: dist=%zu < 2*nn or odd", dist);
+  if (count == 0) return GBFFT_OK;
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  double* d;
+  size_t span = (count - 1) * dist + 2 * nn;
+  TRY(stage_inout(c, g.stage_a, data, span, &d));
+  TRY(fft_lines(c.form(), isign, d, (long long)nn, (long long)count, (long long)(dist / 2)));
+  TRY(unstage(c, data, d, span));
+  return ss.finish(c);
+}
+
+int gbfft_four1_batch(double* const* ptrs, const size_t* nn, size_t count, int isign,
+                      const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  TRY(check_isign(isign));
+  if (count == 0) return GBFFT_OK;
+  if (!ptrs || !nn) return fail(GBFFT_INVALID_ARG, "four1_batch: null arrays");
+  for (size_t t = 0; t < count; ++t) {
+    if (!ptrs[t]) return fail(GBFFT_INVALID_ARG, "four1_batch: null pointer at %zu", t);
+    if (!is_pow2(nn[t]) || ilog2(nn[t]) > kMaxAxisLog)
+      return fail(GBFFT_UNSUPPORTED_SIZE, "four1_batch: nn[%zu]=%zu", t, nn[t]);
+  }
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  // group by size; each group is packed contiguously and runs as one batch
+  std::map<size_t, std::vector<size_t>> groups;
+  size_t total = 0;
+  for (size_t t = 0; t < count; ++t) {
+    groups[nn[t]].push_back(t);
+    total += 2 * nn[t];
+  }
+  TRY(ensure(g.stage_b, total * sizeof(double)));
+  double* packed = (double*)g.stage_b.p;
+  if (!c.dev()) {
+    g.host_pack.resize(total * sizeof(double));
+    double* hp = (double*)g.host_pack.data();
+    size_t off = 0;
+    for (auto& kv : groups)
+      for (size_t t : kv.second) {
+        std::memcpy(hp + off, ptrs[t], 2 * kv.first * sizeof(double));
+        off += 2 * kv.first;
+      }
+    TRY(h2d(packed, hp, total * sizeof(double)));
+  } else {
+    size_t off = 0;
+    for (auto& kv : groups)
+      for (size_t t : kv.second) {
+        TRY(d2d(packed + off, ptrs[t], 2 * kv.first * sizeof(double)));
+        off += 2 * kv.first;
+      }
+  }
+  size_t off = 0;
+  for (auto& kv : groups) {
+    long long L = (long long)kv.first, cnt = (long long)kv.second.size();
+    TRY(fft_lines(c.form(), isign, packed + off, L, cnt, L));
+    off += 2 * kv.first * kv.second.size();
+  }
+  if (!c.dev()) {
+    double* hp = (double*)g.host_pack.data();
+    TRY(d2h(hp, packed, total * sizeof(double)));
+    CK(cudaStreamSynchronize(g.cur));
+    size_t o2 = 0;
+    for (auto& kv : groups)
+      for (size_t t : kv.second) {
+        std::memcpy(ptrs[t], hp + o2, 2 * kv.first * sizeof(double));
+        o2 += 2 * kv.first;
+      }
+  } else {
+    size_t o2 = 0;
+    for (auto& kv : groups)
+      for (size_t t : kv.second) {
+        TRY(d2d(ptrs[t], packed + o2, 2 * kv.first * sizeof(double)));
+        o2 += 2 * kv.first;
+      }
+  }
+  return ss.finish(c);
+}
+
+int gbfft_twofft(const double* data1, const double* data2, double* fft1, double* fft2,
+                 size_t n, const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  if (!data1 || !data2 || !fft1 || !fft2) return fail(GBFFT_INVALID_ARG, "twofft: null pointer");
+  if (!is_pow2(n) || ilog2(n) > kMaxAxisLog)
+    return fail(GBFFT_UNSUPPORTED_SIZE, "twofft: n=%zu must be a power of two", n);
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  const double *d1 = data1, *d2p = data2;
+  double *f1, *f2;
+  if (!c.dev()) {
+    TRY(ensure(g.stage_a, 2 * n * sizeof(double)));
+    TRY(ensure(g.stage_b, 2 * n * sizeof(double)));
+    TRY(ensure(g.stage_c, 2 * n * sizeof(double)));
+    double* in = (double*)g.stage_c.p;
+    TRY(h2d(in, data1, n * sizeof(double)));
+    TRY(h2d(in + n, data2, n * sizeof(double)));
+    d1 = in;
+    d2p = in + n;
+    f1 = (double*)g.stage_a.p;
+    f2 = (double*)g.stage_b.p;
+  } else {
+    f1 = fft1;
+    f2 = fft2;
+  }
+  CK(launch_twofft_pack(d1, d2p, f1, (long long)n, g.cur));
+  g.launches++;
+  TRY(fft_lines(c.form(), 1, f1, (long long)n, 1, (long long)n));
+  CK(launch_twofft_split(f1, f2, (long long)n, g.cur));
+  g.launches++;
+  if (!c.dev()) {
+    TRY(d2h(fft1, f1, 2 * n * sizeof(double)));
+    TRY(d2h(fft2, f2, 2 * n * sizeof(double)));
+  }
+  return ss.finish(c);
+}
+
+int gbfft_realft(double* data, size_t n, int isign, const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  if (!data) return fail(GBFFT_INVALID_ARG, "realft: null data");
+  TRY(check_isign(isign));
+  if (n < 2 || !is_pow2(n) || ilog2(n) > kMaxAxisLog)
+    return fail(GBFFT_UNSUPPORTED_SIZE, "realft: n=%zu must be a power of two >= 2", n);
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  double* d;
+  TRY(stage_inout(c, g.stage_a, data, n, &d));
+  TRY(realft_dev(c.form(), d, (long long)n, isign));
+  TRY(unstage(c, data, d, n));
+  return ss.finish(c);
+}
+
+int gbfft_fourn(double* data, const size_t* nn, size_t nn_len, size_t ndim, int isign,
+                const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  // validate_inputs, src/Fourn.rs:367-378
+  if (!nn || ndim == 0 || ndim > nn_len) return fail(GBFFT_INVALID_ARG, "fourn: invalid dimensions");
+  if (isign != 1 && isign != -1) return fail(GBFFT_INVALID_ARG, "fourn: isign must be 1 or -1");
+  for (size_t i = 0; i < ndim; ++i)
+    if (nn[i] <= 1) return fail(GBFFT_INVALID_ARG, "fourn: invalid dimension size");
+  if (!data) return fail(GBFFT_INVALID_ARG, "fourn: null data");
+  long long dims[16];
+  if (ndim > 16) return fail(GBFFT_UNSUPPORTED_SIZE, "fourn: ndim > 16");
+  size_t total = 1;
+  for (size_t i = 0; i < ndim; ++i) {
+    if (!is_pow2(nn[i]) || ilog2(nn[i]) > kMaxAxisLog)
+      return fail(GBFFT_UNSUPPORTED_SIZE, "fourn: nn[%zu]=%zu must be a power of two", i, nn[i]);
+    dims[i] = (long long)nn[i];
+    total *= nn[i];
+  }
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  double* d;
+  TRY(stage_inout(c, g.stage_a, data, 2 * total, &d));
+  TRY(fourn_dev(c.form(), d, dims, (int)ndim, isign));
+  TRY(unstage(c, data, d, 2 * total));
+  return ss.finish(c);
+}
+
+int gbfft_rlft3(double* data, double* speq, size_t nn1, size_t nn2, size_t nn3, int isign,
+                const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  if (!data || !speq) return fail(GBFFT_INVALID_ARG, "rlft3: null pointer");
+  if (isign != 1 && isign != -1) return fail(GBFFT_INVALID_ARG, "rlft3: isign must be 1 or -1");
+  if (!is_pow2(nn1) || !is_pow2(nn2) || !is_pow2(nn3) || nn3 < 2 ||
+      ilog2(nn1) > kMaxAxisLog || ilog2(nn2) > kMaxAxisLog || ilog2(nn3) > kMaxAxisLog)
+    return fail(GBFFT_UNSUPPORTED_SIZE, "rlft3: dims must be powers of two, nn3 >= 2");
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  Twiddles tw;
+  TRY(tables(c.form(), tw));
+  const size_t total = nn1 * nn2 * nn3;
+  double *d, *sp;
+  TRY(stage_inout(c, g.stage_a, data, total, &d));
+  TRY(stage_inout(c, g.stage_b, speq, 2 * nn1 * nn2, &sp, isign == -1));
+  long long dims[3] = {(long long)nn1, (long long)nn2, (long long)(nn3 / 2)};
+  if (isign == 1) {
+    TRY(fourn_dev(c.form(), d, dims, 3, 1));
+    CK(launch_rlft3_speq(d, sp, nn1, nn2, nn3, g.cur));
+    g.launches++;
+    CK(launch_rlft3_twist(c.form(), 1, d, sp, nn1, nn2, nn3, tw, g.cur));
+    g.launches++;
+  } else {
+    CK(launch_rlft3_twist(c.form(), -1, d, sp, nn1, nn2, nn3, tw, g.cur));
+    g.launches++;
+    TRY(fourn_dev(c.form(), d, dims, 3, -1));
+  }
+  TRY(unstage(c, data, d, total));
+  TRY(unstage(c, speq, sp, 2 * nn1 * nn2));
+  return ss.finish(c);
+}
+
+static int spectral_call(const Call& c, int kind, const double* a, const double* b, size_t n,
+                         size_t m, double* ans) {
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  TRY(ensure(g.work, 2 * n * sizeof(double)));
+  double* w = (double*)g.work.p;
+  const double *da = a, *db = b;
+  if (!c.dev()) {
+    TRY(ensure(g.stage_c, (n + m) * sizeof(double)));
+    double* in = (double*)g.stage_c.p;
+    TRY(h2d(in, a, n * sizeof(double)));
+    TRY(h2d(in + n, b, m * sizeof(double)));
+    da = in;
+    db = in + n;
+  }
+  if (kind == 2) {
+    TRY(d2d(w, da, n * sizeof(double)));
+    TRY(d2d(w + n, db, n * sizeof(double)));
+  } else {
+    CK(launch_expand_response(db, (long long)m, w + n, (long long)n, da, w, g.cur));
+    g.launches++;
+  }
+  TRY(spectral_dev(c.form(), kind, w, (long long)n));
+  if (c.dev()) TRY(d2d(ans, w, n * sizeof(double)));
+  else TRY(d2h(ans, w, n * sizeof(double)));
+  return ss.finish(c);
+}
+
+int gbfft_convlv(const double* data, size_t n, const double* respns, size_t m, int isign,
+                 double* ans, const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  // order of checks as src/Convolve.rs:13-21
+  if (n == 0 || m == 0) return fail(GBFFT_EMPTY_INPUT, "convlv: input arrays cannot be empty");
+  if (m > n) return fail(GBFFT_RESPONSE_TOO_LONG, "convlv: response function longer than data");
+  if (isign != 1 && isign != -1)
+    return fail(GBFFT_INVALID_ISIGN, "convlv: isign must be 1 (convolution) or -1 (deconvolution)");
+  if (!data || !respns || !ans) return fail(GBFFT_INVALID_ARG, "convlv: null pointer");
+  if (n < 2 || !is_pow2(n) || ilog2(n) > kMaxAxisLog)
+    return fail(GBFFT_UNSUPPORTED_SIZE, "convlv: n=%zu must be a power of two >= 2", n);
+  return spectral_call(c, isign == 1 ? 0 : 1, data, respns, n, m, ans);
+}
+
+int gbfft_correl(const double* data1, size_t n1, const double* data2, size_t n2, double* ans,
+                 const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  if (n1 == 0) return fail(GBFFT_EMPTY_INPUT, "correl: input arrays cannot be empty");
+  if (n2 != n1) return fail(GBFFT_LENGTH_MISMATCH, "correl: input arrays must have the same length");
+  if (!data1 || !data2 || !ans) return fail(GBFFT_INVALID_ARG, "correl: null pointer");
+  const size_t n = n1;
+  if (n <= 32) {
+    TRY(init_locked(g.device));
+    StreamScope ss(c);
+    const double *a = data1, *b = data2;
+    double* out = ans;
+    if (!c.dev()) {
+      TRY(ensure(g.stage_c, 3 * n * sizeof(double)));
+      double* in = (double*)g.stage_c.p;
+      TRY(h2d(in, data1, n * sizeof(double)));
+      TRY(h2d(in + n, data2, n * sizeof(double)));
+      a = in;
+      b = in + n;
+      out = in + 2 * n;
+    }
+    CK(launch_correl_direct(a, b, out, (long long)n, g.cur));
+    g.launches++;
+    if (!c.dev()) TRY(d2h(ans, out, n * sizeof(double)));
+    return ss.finish(c);
+  }
+  if (!is_pow2(n) || ilog2(n) > kMaxAxisLog)
+    return fail(GBFFT_UNSUPPORTED_SIZE, "correl: n=%zu must be a power of two when > 32", n);
+  return spectral_call(c, 2, data1, data2, n, n, ans);
+}
+
+static int spectrum_call(int kind, const double* cdata, size_t nn, double* out,
+                         const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  if (!cdata || !out) return fail(GBFFT_INVALID_ARG, "spectrum: null pointer");
+  if (nn == 0) return GBFFT_OK;
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  const double* in = cdata;
+  double* o = out;
+  if (!c.dev()) {
+    TRY(ensure(g.stage_c, 3 * nn * sizeof(double)));
+    double* s = (double*)g.stage_c.p;
+    TRY(h2d(s, cdata, 2 * nn * sizeof(double)));
+    in = s;
+    o = s + 2 * nn;
+  }
+  CK(launch_spectrum(kind, in, o, (long long)nn, g.cur));
+  g.launches++;
+  if (!c.dev()) TRY(d2h(out, o, nn * sizeof(double)));
+  return ss.finish(c);
+}
+
+int gbfft_magnitude_spectrum(const double* c, size_t nn, double* out, const gbfft_opts* opts) {
+  return spectrum_call(0, c, nn, out, opts);
+}
+int gbfft_power_spectrum(const double* c, size_t nn, double* out, const gbfft_opts* opts) {
+  return spectrum_call(1, c, nn, out, opts);
+}
+
+int gbfft_sinft(double* y, size_t n, const gbfft_opts* opts) {
+  (void)y; (void)n; (void)opts;
+  return fail(GBFFT_UNSUPPORTED_SIZE, "sinft: not built yet");
+}
+int gbfft_cosft1(double* y, size_t n, const gbfft_opts* opts) {
+  (void)y; (void)n; (void)opts;
+  return fail(GBFFT_UNSUPPORTED_SIZE, "cosft1: not built yet");
+}
+int gbfft_cosft2(double* y, size_t n, int isign, const gbfft_opts* opts) {
+  (void)y; (void)n; (void)isign; (void)opts;
+  return fail(GBFFT_UNSUPPORTED_SIZE, "cosft2: not built yet");
+}
+
+}  // extern "C"

@@ -1,0 +1,476 @@
+// spectral.cu -- the real-data and spectral kernels around the complex passes:
+// twiddle tables, the realft twist, the fused convlv/correl spectral step,
+// the response expansion, the small-n direct correlation, twofft, rlft3 and
+// the sine/cosine transform pre/post passes.
+//
+// Index conventions are 0-based restatements of the Numerical Recipes
+// routines the reference crate follows (file:line at each kernel).
+#include "arith.cuh"
+#include "fft_core.cuh"
+#include "gbfft_internal.h"
+
+namespace gbfft {
+
+// ---------------------------------------------------------------------------
+// Twiddle tables: exp(+2 pi i e / S) from sincospi in double, stored in the
+// form's twiddle element.
+// ---------------------------------------------------------------------------
+template <class F>
+__device__ __forceinline__ void put_tw(typename F::TW* t, size_t i, double c, double s) {
+  if constexpr (F::kind == 0) {
+    t[i] = d2{c, s};
+  } else if constexpr (F::kind == 1) {
+    t[i] = f2{(float)c, (float)s};
+  } else {
+    float ch = (float)c, sh = (float)s;
+    t[i] = f4{ch, (float)(c - (double)ch), sh, (float)(s - (double)sh)};
+  }
+}
+
+template <class F>
+__global__ void k_twiddles(typename F::TW* dense, typename F::TW* partial) {
+  const size_t total = kDenseEntries + kPartialEntries;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    double c, s;
+    if (i < kDenseEntries) {
+      // entry S + e of level S: S = highest power of two <= i
+      if (i < 2) {
+        c = 1.0; s = 0.0;
+      } else {
+        int logS = 63 - __clzll((long long)i);
+        long long S = 1ll << logS;
+        long long e = (long long)i - S;
+        sincospi(2.0 * (double)e / (double)S, &s, &c);
+      }
+      put_tw<F>(dense, i, c, s);
+    } else {
+      size_t j = i - kDenseEntries;
+      int lvl = (int)(j >> kPartialLog) + kDenseLog + 1;
+      long long e = (long long)(j & (kPartial - 1));
+      sincospi(2.0 * (double)e / (double)(1ll << lvl), &s, &c);
+      put_tw<F>(partial, j, c, s);
+    }
+  }
+}
+
+cudaError_t launch_twiddles(Form f, void* dense, void* partial, cudaStream_t st) {
+  dim3 g(1024), b(256);
+  if (f == FORM_F64) k_twiddles<F64><<<g, b, 0, st>>>((d2*)dense, (d2*)partial);
+  else if (f == FORM_F32) k_twiddles<F32><<<g, b, 0, st>>>((f2*)dense, (f2*)partial);
+  else k_twiddles<DF64><<<g, b, 0, st>>>((f4*)dense, (f4*)partial);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// realft twist (src/Real_FT.rs:24-213 restated 0-based).  For the pair of
+// complex slots k and m = n/2 - k of the n/2-point spectrum Z:
+//   h1 = (Z_k + conj Z_m)/2,  h2 = -isign * i (Z_k - conj Z_m)/2,
+//   t = w^k h2 with w = exp(isign 2 pi i / n),
+//   Z_k <- h1 + t,  Z_m <- conj(h1 - t).
+// Slot 0 packs DC and Nyquist; slot n/4 is left unchanged (the reference
+// loop stops at n/4 - 1 as well).
+// ---------------------------------------------------------------------------
+template <class F, int IS>
+__device__ __forceinline__ void twist_pair(typename F::C& zk, typename F::C& zm,
+                                           typename F::C w) {
+  using C = typename F::C;
+  C czm = F::conj(zm);
+  C h1 = F::scale(F::add(zk, czm), 0.5);
+  C h2 = F::scale(F::mul_j(F::sub(zk, czm), -IS), 0.5);
+  C t = F::mul(h2, w);
+  zk = F::add(h1, t);
+  zm = F::conj(F::sub(h1, t));
+}
+
+template <class F>
+__device__ __forceinline__ typename F::C ldc(const double* p, long long k) {
+  d2 v = reinterpret_cast<const d2*>(p)[k];
+  return F::from_d(v.x, v.y);
+}
+template <class F>
+__device__ __forceinline__ void stc(double* p, long long k, typename F::C a) {
+  double x, y;
+  F::to_d(a, x, y);
+  reinterpret_cast<d2*>(p)[k] = d2{x, y};
+}
+
+template <class F, int IS>
+__global__ void k_realft_twist(double* data, long long n, long long batch, long long dist,
+                               Twiddles tw) {
+  const long long nq = n / 4;  // pairs k = 1..nq-1, plus slot 0
+  const long long per = nq > 0 ? nq : 1;
+  const int logn = 63 - __clzll(n);
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < per * batch;
+       g += (long long)gridDim.x * blockDim.x) {
+    const long long bidx = g / per;
+    const long long k = g - bidx * per;
+    double* d = data + bidx * dist;
+    if (k == 0) {
+      if (IS > 0) {
+        double h = d[0], v = d[1];
+        d[0] = h + v;
+        d[1] = h - v;
+      } else {
+        double h = d[0], v = d[1];
+        d[0] = 0.5 * (h + v);
+        d[1] = 0.5 * (h - v);
+      }
+      continue;
+    }
+    const long long m = n / 2 - k;
+    typename F::C zk = ldc<F>(d, k), zm = ldc<F>(d, m);
+    typename F::C w = twiddle<F>(tw, logn, k, IS);
+    twist_pair<F, IS>(zk, zm, w);
+    stc<F>(d, k, zk);
+    stc<F>(d, m, zm);
+  }
+}
+
+cudaError_t launch_realft_twist(Form f, int isign, double* data, long long n, long long batch,
+                                long long dist, Twiddles tw, cudaStream_t st) {
+  long long work = (n / 4 > 0 ? n / 4 : 1) * batch;
+  int blocks = (int)((work + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+#define TW_LAUNCH(FT)                                                                    \
+  (isign > 0 ? (k_realft_twist<FT, 1><<<blocks, 256, 0, st>>>(data, n, batch, dist, tw)) \
+             : (k_realft_twist<FT, -1><<<blocks, 256, 0, st>>>(data, n, batch, dist, tw)))
+  if (f == FORM_F64) TW_LAUNCH(F64);
+  else if (f == FORM_F32) TW_LAUNCH(F32);
+  else TW_LAUNCH(DF64);
+#undef TW_LAUNCH
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Fused convlv / correl spectral step (src/Convolve.rs:90-138,
+// src/Correlation.rs:68-110; products at Convolve.rs:112-128 and
+// Correlation.rs:90-96).  a and b hold the raw n/2-point complex FFTs of the
+// two real inputs (forward, isign=+1).  Per pair (k, n/2-k): forward twist of
+// both, product scaled by 1/(n/2), inverse twist -- the packed input of the
+// inverse n/2-point FFT, written to out (which may alias a).
+// ---------------------------------------------------------------------------
+template <class F, int KIND>
+__device__ __forceinline__ typename F::C spec_prod(typename F::C x, typename F::C y, double inv_no2) {
+  using C = typename F::C;
+  if constexpr (KIND == 0) {
+    return F::scale(F::mul(x, y), inv_no2);
+  } else if constexpr (KIND == 2) {
+    return F::scale(F::mul(x, F::conj(y)), inv_no2);
+  } else {
+    // deconvolution in double: zero where |y|^2 < 1e-12 (src/Convolve.rs:118-122)
+    double xr, xi, yr, yi;
+    F::to_d(x, xr, xi);
+    F::to_d(y, yr, yi);
+    double mag2 = yr * yr + yi * yi;
+    double o_r = 0.0, o_i = 0.0;
+    if (!(mag2 < 1e-12)) {
+      o_r = (xr * yr + xi * yi) / mag2 * inv_no2;
+      o_i = (xi * yr - xr * yi) / mag2 * inv_no2;
+    }
+    return F::from_d(o_r, o_i);
+  }
+}
+
+template <class F, int KIND>
+__device__ __forceinline__ double spec_prod_real(double x, double y, double inv_no2) {
+  if constexpr (KIND == 1) {
+    double mag2 = y * y;
+    return (mag2 < 1e-12) ? 0.0 : (x * y) / mag2 * inv_no2;
+  } else {
+    return x * y * inv_no2;
+  }
+}
+
+template <class F, int KIND>
+__global__ void k_spectral(const double* a, const double* b, double* out, long long n,
+                           Twiddles tw) {
+  using C = typename F::C;
+  const long long nq = n / 4;
+  const long long per = nq > 0 ? nq : 1;
+  const double inv_no2 = 2.0 / (double)n;
+  const int logn = 63 - __clzll(n);
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k <= per;
+       k += (long long)gridDim.x * blockDim.x) {
+    if (k == 0) {
+      // DC in slot 0 real part, Nyquist in slot 0 imaginary part after the twist
+      double a0 = a[0], a1 = a[1], b0 = b[0], b1 = b[1];
+      double ad = a0 + a1, an = a0 - a1, bd = b0 + b1, bn = b0 - b1;
+      if (n == 2) {  // the n/2 = 1 point "FFT" holds (x0 + x1) + i 0
+        ad = a0 + a1; an = a0 - a1;
+      }
+      double pd = spec_prod_real<F, KIND>(ad, bd, inv_no2);
+      double pn = spec_prod_real<F, KIND>(an, bn, inv_no2);
+      out[0] = 0.5 * (pd + pn);
+      out[1] = 0.5 * (pd - pn);
+      continue;
+    }
+    if (k > nq) continue;
+    if (k == nq) {
+      // middle slot n/4: both twists are the identity
+      C x = ldc<F>(a, k), y = ldc<F>(b, k);
+      stc<F>(out, k, spec_prod<F, KIND>(x, y, inv_no2));
+      continue;
+    }
+    const long long m = n / 2 - k;
+    C ak = ldc<F>(a, k), am = ldc<F>(a, m), bk = ldc<F>(b, k), bm = ldc<F>(b, m);
+    C w = twiddle<F>(tw, logn, k, 1);
+    twist_pair<F, 1>(ak, am, w);
+    twist_pair<F, 1>(bk, bm, w);
+    C pk = spec_prod<F, KIND>(ak, bk, inv_no2);
+    C pm = spec_prod<F, KIND>(am, bm, inv_no2);
+    twist_pair<F, -1>(pk, pm, F::conj(w));
+    stc<F>(out, k, pk);
+    stc<F>(out, m, pm);
+  }
+}
+
+cudaError_t launch_spectral_product(Form f, int kind, const double* a, const double* b,
+                                    double* out, long long n, Twiddles tw, cudaStream_t st) {
+  long long work = n / 4 + 1;
+  int blocks = (int)((work + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+#define SP_LAUNCH(FT)                                                                      \
+  switch (kind) {                                                                          \
+    case 0: k_spectral<FT, 0><<<blocks, 256, 0, st>>>(a, b, out, n, tw); break;            \
+    case 1: k_spectral<FT, 1><<<blocks, 256, 0, st>>>(a, b, out, n, tw); break;            \
+    default: k_spectral<FT, 2><<<blocks, 256, 0, st>>>(a, b, out, n, tw); break;           \
+  }
+  if (f == FORM_F64) { SP_LAUNCH(F64) }
+  else if (f == FORM_F32) { SP_LAUNCH(F32) }
+  else { SP_LAUNCH(DF64) }
+#undef SP_LAUNCH
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Response expansion (Numerical Recipes convlv contract): r[0..m) = respns,
+// r[n-k] = respns[m-k] for k = 1..(m-1)/2, zeros in [(m+1)/2, n-(m-1)/2).
+// ---------------------------------------------------------------------------
+__global__ void k_expand(const double* respns, long long m, double* dst, long long n,
+                         const double* data, double* dst_data) {
+  const long long half = (m - 1) / 2;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double v;
+    if (half > 0 && i >= n - half) v = respns[m - (n - i)];
+    else if (i < (m + 1) / 2) v = respns[i];
+    else v = 0.0;
+    dst[i] = v;
+    if (dst_data) dst_data[i] = data[i];
+  }
+}
+
+cudaError_t launch_expand_response(const double* respns, long long m, double* dst, long long n,
+                                   const double* data, double* dst_data, cudaStream_t st) {
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_expand<<<blocks, 256, 0, st>>>(respns, m, dst, n, data, dst_data);
+  return cudaGetLastError();
+}
+
+// Direct linear correlation, the reference's n <= 32 branch
+// (src/Correlation.rs:37-50): out[lag] = sum_{i < n-lag} a[i+lag] b[i].
+__global__ void k_correl_direct(const double* a, const double* b, double* out, long long n) {
+  long long lag = threadIdx.x;
+  if (lag >= n) return;
+  double sum = 0.0;
+  for (long long i = 0; i < n - lag; ++i) sum += a[i + lag] * b[i];
+  out[lag] = sum;
+}
+
+cudaError_t launch_correl_direct(const double* a, const double* b, double* out, long long n,
+                                 cudaStream_t st) {
+  k_correl_direct<<<1, 32, 0, st>>>(a, b, out, n);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// twofft (src/FFT_2.rs:3-132, Numerical Recipes contract): pack data1 + i
+// data2, and after the n-point FFT split the spectrum into the two real
+// inputs' spectra; the mirror of slot k is n-k.
+// ---------------------------------------------------------------------------
+__global__ void k_twofft_pack(const double* d1, const double* d2v, double* fft1, long long n) {
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
+       j += (long long)gridDim.x * blockDim.x) {
+    reinterpret_cast<d2*>(fft1)[j] = d2{d1[j], d2v[j]};
+  }
+}
+
+__global__ void k_twofft_split(double* fft1, double* fft2, long long n) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k <= n / 2;
+       k += (long long)gridDim.x * blockDim.x) {
+    if (k == 0) {
+      fft2[0] = fft1[1];
+      fft1[1] = 0.0;
+      fft2[1] = 0.0;
+      continue;
+    }
+    const long long j = 2 * k, jr = 2 * n - 2 * k;
+    double rep = 0.5 * (fft1[j] + fft1[jr]);
+    double rem = 0.5 * (fft1[j] - fft1[jr]);
+    double aip = 0.5 * (fft1[j + 1] + fft1[jr + 1]);
+    double aim = 0.5 * (fft1[j + 1] - fft1[jr + 1]);
+    fft1[j] = rep;
+    fft1[j + 1] = aim;
+    fft1[jr] = rep;
+    fft1[jr + 1] = -aim;
+    fft2[j] = aip;
+    fft2[j + 1] = -rem;
+    fft2[jr] = aip;
+    fft2[jr + 1] = rem;
+  }
+}
+
+cudaError_t launch_twofft_pack(const double* d1, const double* d2v, double* fft1, long long n,
+                               cudaStream_t st) {
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_twofft_pack<<<blocks, 256, 0, st>>>(d1, d2v, fft1, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_twofft_split(double* fft1, double* fft2, long long n, cudaStream_t st) {
+  long long work = n / 2 + 1;
+  int blocks = (int)((work + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_twofft_split<<<blocks, 256, 0, st>>>(fft1, fft2, n);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// rlft3 (src/Real_FT3.rs:8-141, Numerical Recipes contract).  data is
+// nn1 x nn2 x nn3 reals = nn1 x nn2 x nh complex (nh = nn3/2); speq is
+// nn1 x nn2 complex.  After the forward 3-D FFT, speq takes the k3 = 0 plane.
+// ---------------------------------------------------------------------------
+__global__ void k_rlft3_speq(const double* data, double* speq, long long nn1, long long nn2,
+                             long long nn3) {
+  const long long total = nn1 * nn2;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    reinterpret_cast<d2*>(speq)[g] = reinterpret_cast<const d2*>(data)[g * (nn3 / 2)];
+  }
+}
+
+cudaError_t launch_rlft3_speq(const double* data, double* speq, long long nn1, long long nn2,
+                              long long nn3, cudaStream_t st) {
+  long long total = nn1 * nn2;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_rlft3_speq<<<blocks, 256, 0, st>>>(data, speq, nn1, nn2, nn3);
+  return cudaGetLastError();
+}
+
+// The twist pairs element (i1, i2, i3) with (j1, j2, nh - i3), j = mirrored
+// indices; i3 = 0 pairs with the speq entry (j1, j2).  Each unordered pair is
+// handled by exactly one thread: i3 in 1..nh/2-1 own their pair outright; at
+// i3 = 0 and i3 = nh/2 the pair partner lies in the same plane, so the thread
+// with the lexicographically smaller (i1, i2) owns it.
+// Forward (isign=+1) and inverse share the formulas of the reference loop
+// (src/Real_FT3.rs:60-127) with c2 = -isign/2 and w = exp(isign 2 pi i i3/nn3).
+template <class F, int IS>
+__global__ void k_rlft3_twist(double* data, double* speq, long long nn1, long long nn2,
+                              long long nn3, Twiddles tw) {
+  using C = typename F::C;
+  const long long nh = nn3 / 2;
+  // planes i3 = 0 .. nh/2-1; the middle plane i3 = nh/2 maps onto itself and
+  // the twist there is the identity (w = isign*i makes h1 + w h2 = Z_k).
+  const long long planes = nh >= 2 ? nh / 2 : 1;
+  const long long total = nn1 * nn2 * planes;
+  const int logn3 = 63 - __clzll(nn3);
+  d2* sp = reinterpret_cast<d2*>(speq);
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    const long long i3 = g % planes;
+    const long long i12 = g / planes;
+    const long long i2 = i12 % nn2, i1 = i12 / nn2;
+    const long long j1 = i1 ? nn1 - i1 : 0, j2 = i2 ? nn2 - i2 : 0;
+    const long long self = i1 * nn2 + i2, mate = j1 * nn2 + j2;
+    if (i3 == 0) {
+      // data(i1,i2,0) pairs with speq(j1,j2) and data(j1,j2,0) with
+      // speq(i1,i2); the thread with the smaller line index does both.
+      if (mate < self) continue;
+      const C one = F::from_d(1.0, 0.0);
+      C zk = ldc<F>(data, self * nh);
+      C zs = F::from_d(sp[mate].x, sp[mate].y);
+      C zk2 = zk, zs2 = zs;
+      if (mate != self) {
+        zk2 = ldc<F>(data, mate * nh);
+        zs2 = F::from_d(sp[self].x, sp[self].y);
+      }
+      twist_pair<F, IS>(zk, zs, one);
+      double x, y;
+      if (mate != self) {
+        twist_pair<F, IS>(zk2, zs2, one);
+        stc<F>(data, mate * nh, zk2);
+        F::to_d(zs2, x, y);
+        sp[self] = d2{x, y};
+      }
+      stc<F>(data, self * nh, zk);
+      F::to_d(zs, x, y);
+      sp[mate] = d2{x, y};
+      continue;
+    }
+    const long long i3m = nh - i3;
+    C w = twiddle<F>(tw, logn3, i3, IS);
+    C zk = ldc<F>(data, self * nh + i3);
+    C zm = ldc<F>(data, mate * nh + i3m);
+    twist_pair<F, IS>(zk, zm, w);
+    stc<F>(data, self * nh + i3, zk);
+    stc<F>(data, mate * nh + i3m, zm);
+  }
+}
+
+cudaError_t launch_rlft3_twist(Form f, int isign, double* data, double* speq, long long nn1,
+                               long long nn2, long long nn3, Twiddles tw, cudaStream_t st) {
+  long long total = nn1 * nn2 * (nn3 / 4 > 0 ? nn3 / 4 : 1);
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+#define R3_LAUNCH(FT)                                                                       \
+  (isign > 0 ? (k_rlft3_twist<FT, 1><<<blocks, 256, 0, st>>>(data, speq, nn1, nn2, nn3, tw)) \
+             : (k_rlft3_twist<FT, -1><<<blocks, 256, 0, st>>>(data, speq, nn1, nn2, nn3, tw)))
+  if (f == FORM_F64) R3_LAUNCH(F64);
+  else if (f == FORM_F32) R3_LAUNCH(F32);
+  else R3_LAUNCH(DF64);
+#undef R3_LAUNCH
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Element-wise helpers.
+// ---------------------------------------------------------------------------
+__global__ void k_scale(double* d, long long count, double s) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x)
+    d[i] *= s;
+}
+
+cudaError_t launch_scale(double* data, long long count, double s, cudaStream_t st) {
+  int blocks = (int)((count + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  k_scale<<<blocks, 256, 0, st>>>(data, count, s);
+  return cudaGetLastError();
+}
+
+// magnitude_spectrum / power_spectrum (src/FFT_1.rs:206-228)
+__global__ void k_spectrum(int kind, const double* c, double* out, long long nn) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nn;
+       i += (long long)gridDim.x * blockDim.x) {
+    d2 v = reinterpret_cast<const d2*>(c)[i];
+    double p = v.x * v.x + v.y * v.y;
+    out[i] = kind == 0 ? sqrt(p) : p;
+  }
+}
+
+cudaError_t launch_spectrum(int kind, const double* c, double* out, long long nn,
+                            cudaStream_t st) {
+  int blocks = (int)((nn + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  k_spectrum<<<blocks, 256, 0, st>>>(kind, c, out, nn);
+  return cudaGetLastError();
+}
+
+}  // namespace gbfft

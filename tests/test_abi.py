@@ -1,0 +1,86 @@
+"""CPU tests of the C-ABI library: it loads, exports every entry point that
+include/gbfft.h declares, and rejects bad arguments before touching a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", f) for f in sorted(os.listdir(os.path.join(ROOT, "include")))
+           if f.endswith(".h")]
+
+
+def declared_symbols():
+    names = []
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"\b(gbfft_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from numrs_gb300 import build, _lib
+    build.build()
+    return _lib.load()
+
+
+def test_header_declares_the_family():
+    syms = declared_symbols()
+    for name in ("gbfft_four1", "gbfft_four1_batch", "gbfft_twofft", "gbfft_realft",
+                 "gbfft_fourn", "gbfft_rlft3", "gbfft_sinft", "gbfft_cosft1", "gbfft_cosft2",
+                 "gbfft_convlv", "gbfft_correl"):
+        assert name in syms
+
+
+def test_every_declared_symbol_is_exported(lib):
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_argument_errors_need_no_gpu(lib):
+    from numrs_gb300 import _lib as L
+    x = np.zeros(8)
+    p = x.ctypes.data
+    # convlv check order, src/Convolve.rs:13-21
+    assert lib.gbfft_convlv(p, 0, p, 1, 1, p, None) == L.EMPTY_INPUT
+    assert lib.gbfft_convlv(p, 2, p, 3, 1, p, None) == L.RESPONSE_TOO_LONG
+    assert lib.gbfft_convlv(p, 2, p, 1, 0, p, None) == L.INVALID_ISIGN
+    assert lib.gbfft_convlv(p, 6, p, 1, 1, p, None) == L.UNSUPPORTED_SIZE
+    # correl, src/Correlation.rs:10-16
+    assert lib.gbfft_correl(p, 0, p, 1, p, None) == L.EMPTY_INPUT
+    assert lib.gbfft_correl(p, 2, p, 1, p, None) == L.LENGTH_MISMATCH
+    # fourn validate_inputs, src/Fourn.rs:367-378
+    nn = (ctypes.c_size_t * 2)(8, 1)
+    assert lib.gbfft_fourn(p, nn, 2, 2, 1, None) == L.INVALID_ARG
+    assert lib.gbfft_fourn(p, nn, 2, 3, 1, None) == L.INVALID_ARG
+    assert lib.gbfft_fourn(p, nn, 2, 1, 0, None) == L.INVALID_ARG
+    # sizes and signs
+    assert lib.gbfft_four1(p, 3, 1, None) == L.UNSUPPORTED_SIZE
+    assert lib.gbfft_four1(p, 4, 2, None) == L.INVALID_ARG
+    assert lib.gbfft_four1(None, 4, 1, None) == L.INVALID_ARG
+    assert lib.gbfft_realft(p, 6, 1, None) == L.UNSUPPORTED_SIZE
+    assert lib.gbfft_rlft3(p, p, 2, 2, 2, 0, None) == L.INVALID_ARG
+    msg = L.last_error()
+    assert "isign" in msg
+
+
+def test_python_mirror_raises_reference_errors(lib):
+    import numrs_gb300 as nr
+    with pytest.raises(nr.ConvlvError.EmptyInput):
+        nr.convlv([], [1.0], 1)
+    with pytest.raises(nr.ConvlvError.ResponseTooLong):
+        nr.convlv([1.0, 2.0], [1.0, 2.0, 3.0], 1)
+    with pytest.raises(nr.ConvlvError.InvalidIsign):
+        nr.convlv([1.0, 2.0], [1.0], 0)
+    with pytest.raises(nr.CorrelError.EmptyInput):
+        nr.correl([], [1.0])
+    with pytest.raises(nr.CorrelError.LengthMismatch):
+        nr.correl([1.0, 2.0], [1.0])
+    with pytest.raises(ValueError):
+        nr.fourn(np.zeros(4), [1], 1, 1)
+    with pytest.raises(ValueError):
+        nr.cosft2(np.zeros(8), 8, 0)

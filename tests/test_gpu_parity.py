@@ -1,0 +1,293 @@
+"""GPU parity: every routine through the C ABI against the CPU oracle.
+
+Bars (written into each check):
+  FP64 and DF64 forms: rel-L2 <= 1e-12 and max-abs <= 1e-12 * ||X_ref||_inf * log2 N
+  FP32 form:           rel-L2 <= 1e-6
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from numrs_gb300 import workloads as W
+from conftest import rel_l2, assert_fp64_close
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "golden.npz")
+FORMS = ["fp64", "df64", "fp32"]
+
+
+@pytest.fixture(scope="module")
+def nr():
+    import numrs_gb300
+    from numrs_gb300 import build
+    build.build()
+    return numrs_gb300
+
+
+def check(got, ref, log2n, form, what=""):
+    if form == "fp32":
+        e = rel_l2(got, ref)
+        assert e <= 1e-6, "%s fp32 rel-L2 %.3e > 1e-6" % (what, e)
+    else:
+        assert_fp64_close(got, ref, log2n, "%s %s" % (what, form))
+
+
+def oracle_four1(x, nn, isign):
+    d = x.copy()
+    O.four1(d, nn, isign)
+    return d
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("log2n", list(range(0, 15)))
+def test_four1_small_sizes(nr, form, log2n):
+    nn = 1 << log2n
+    for isign in (1, -1):
+        x = W.uniform_pm1(1000 + log2n, 2 * nn)
+        d = x.copy()
+        nr.four1(d, nn, isign, form=form)
+        check(d, oracle_four1(x, nn, isign), log2n, form, "four1 nn=%d isign=%d" % (nn, isign))
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("log2n", [13, 15, 16, 19, 20, 22])
+def test_four1_multipass(nr, form, log2n):
+    nn = 1 << log2n
+    x = W.normal(2000 + log2n, 2 * nn)
+    d = x.copy()
+    nr.four1(d, nn, 1, form=form)
+    check(d, oracle_four1(x, nn, 1), log2n, form, "four1 nn=%d" % nn)
+
+
+def test_four1_roundtrip_c1(nr):
+    # the N=4096 configuration: +1 then -1, scaled by 1/N
+    x = W.four1_c1()
+    d = x.copy()
+    nr.four1(d, 4096, 1)
+    nr.four1(d, 4096, -1)
+    d /= 4096
+    assert_fp64_close(d, x, 12, "four1 round trip")
+
+
+def test_four1_device_tensor(nr):
+    torch = pytest.importorskip("torch")
+    nn = 1 << 12
+    x = W.normal(7, 2 * nn)
+    t = torch.from_numpy(x.copy()).cuda()
+    nr.four1(t, nn, 1)
+    torch.cuda.synchronize()
+    assert_fp64_close(t.cpu().numpy(), oracle_four1(x, nn, 1), 12, "four1 tensor")
+
+
+def test_four1_golden(nr):
+    g = np.load(GOLD)
+    d = g["four1_4096_in"].copy()
+    nr.four1(d, 4096, 1)
+    assert_fp64_close(d, g["four1_4096_out_p"], 12, "golden four1 +1")
+    d = g["four1_4096_in"].copy()
+    nr.four1(d, 4096, -1)
+    assert_fp64_close(d, g["four1_4096_out_m"], 12, "golden four1 -1")
+    for nn in (1, 2, 4, 8, 16, 32, 64, 128):
+        d = g["four1_small_%d_in" % nn].copy()
+        nr.four1(d, nn, 1)
+        assert_fp64_close(d, g["four1_small_%d_out" % nn], max(1, nn.bit_length() - 1), "golden small")
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_four1_many(nr, form):
+    nn, count = 256, 37
+    x = W.normal(11, 2 * nn * count)
+    d = x.copy()
+    nr.four1_many(d, nn, count, 1, form=form)
+    ref = x.copy().reshape(count, 2 * nn)
+    for r in ref:
+        O.four1(r, nn, 1)
+    check(d, ref.ravel(), 8, form, "four1_many")
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_fft_batch_uneven(nr, form):
+    sizes, u = W.batch_c3(count=300)
+    data = W.batch_c3_data(sizes, u)
+    work = [a.copy() for a in data]
+    nr.FFTProcessor(form=form).fft_batch(work, 1)
+    for a, w, s in zip(data, work, sizes):
+        ref = a.copy()
+        (O.four1_optimized if s >= 512 else O.four1)(ref, int(s), 1)
+        check(w, ref, int(s).bit_length() - 1, form, "fft_batch nn=%d" % s)
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("log2n", [1, 2, 3, 4, 8, 10, 12, 13, 16, 20])
+def test_realft(nr, form, log2n):
+    n = 1 << log2n
+    x = W.normal(3000 + log2n, n)
+    d = x.copy()
+    nr.realft(d, n, 1, form=form)
+    ref = x.copy()
+    O.realft(ref, n, 1)
+    check(d, ref, log2n, form, "realft n=%d" % n)
+    # inverse from the oracle's spectrum
+    d2 = ref.copy()
+    nr.realft(d2, n, -1, form=form)
+    ref2 = ref.copy()
+    O.realft(ref2, n, -1)
+    check(d2, ref2, log2n, form, "realft inverse n=%d" % n)
+
+
+def test_realft_golden(nr):
+    g = np.load(GOLD)
+    d = g["realft_1024_in"].copy()
+    nr.realft(d, 1024, 1)
+    assert_fp64_close(d, g["realft_1024_out"], 10, "golden realft")
+
+
+@pytest.mark.parametrize("n", [4, 256, 4096])
+def test_twofft(nr, n):
+    a, b = W.normal(5, n), W.normal(6, n)
+    f1 = np.full(2 * n + 2, 7.0)
+    f2 = np.full(2 * n + 2, 7.0)
+    nr.twofft(a, b, f1, f2)
+    r1, r2 = O.twofft(a, b)
+    log2n = n.bit_length() - 1
+    assert_fp64_close(f1[:2 * n], r1[:2 * n], log2n, "twofft fft1")
+    assert_fp64_close(f2[:2 * n], r2[:2 * n], log2n, "twofft fft2")
+    assert f1[2 * n] == 7.0 and f2[2 * n + 1] == 7.0  # tail left untouched
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("shape", [(8, 16, 32), (4, 4), (2, 8192), (8192, 4), (64, 2, 128), (16, 16, 16, 16)])
+def test_fourn(nr, form, shape):
+    total = int(np.prod(shape))
+    x = W.uniform_pm1(total, 2 * total)
+    for isign in (1, -1):
+        d = x.copy()
+        nr.fourn(d, shape, len(shape), isign, form=form)
+        ref = x.copy()
+        assert O.fourn(ref, shape, isign) == 0
+        check(d, ref, int(np.log2(total)), form, "fourn %s" % (shape,))
+
+
+def test_fourn_golden(nr):
+    g = np.load(GOLD)
+    d = g["fourn_8x16x32_in"].copy()
+    nr.fourn(d, (8, 16, 32), 3, 1)
+    assert_fp64_close(d, g["fourn_8x16x32_out"], 12, "golden fourn")
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("shape", [(8, 8, 16), (4, 8, 16), (2, 4, 2), (1, 1, 8), (16, 8, 4), (8, 4, 64)])
+def test_rlft3(nr, form, shape):
+    n1, n2, n3 = shape
+    x = W.plane_waves(shape, count=4).ravel()
+    d = x.copy()
+    sp = np.zeros(n1 * 2 * n2)
+    nr.rlft3(d, sp, n1, n2, n3, 1, form=form)
+    rd, rs = x.copy(), np.zeros(n1 * 2 * n2)
+    O.rlft3(rd, rs, n1, n2, n3, 1)
+    log2n = int(np.log2(n1 * n2 * n3))
+    check(d, rd, log2n, form, "rlft3 fwd data")
+    check(sp, rs, log2n, form, "rlft3 fwd speq")
+    d2, s2 = rd.copy(), rs.copy()
+    nr.rlft3(d2, s2, n1, n2, n3, -1, form=form)
+    O.rlft3(rd, rs, n1, n2, n3, -1)
+    check(d2, rd, log2n, form, "rlft3 inverse")
+
+
+def test_rlft3_golden(nr):
+    g = np.load(GOLD)
+    d = g["rlft3_8x8x16_in"].copy()
+    sp = np.zeros(128)
+    nr.rlft3(d, sp, 8, 8, 16, 1)
+    assert_fp64_close(d, g["rlft3_8x8x16_out"], 10, "golden rlft3")
+    assert_fp64_close(sp, g["rlft3_8x8x16_speq"], 10, "golden rlft3 speq")
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("n,m", [(16, 5), (1024, 257), (4096, 3), (64, 64), (8, 1), (32, 4), (2, 1), (4, 3)])
+def test_convlv(nr, form, n, m):
+    x = W.normal(n + 1, n)
+    r = W.normal(m + 2, m)
+    got = nr.convlv(x, r, 1, form=form)
+    st, ref = O.convlv(x, r, 1)
+    assert st == 0
+    check(got, ref, max(1, n.bit_length() - 1), form, "convlv n=%d m=%d" % (n, m))
+    got2 = nr.convlv(ref, r, -1, form=form)
+    st, ref2 = O.convlv(ref, r, -1)
+    check(got2, ref2, max(1, n.bit_length() - 1), form, "deconvolve n=%d m=%d" % (n, m))
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_convlv_c2_full_size(nr, form):
+    # N = 2^20 signal, m = 257 taps in a length-N wrap-around buffer
+    x, r = W.convlv_c2()
+    got = nr.convlv(x, r, 1, form=form)
+    st, ref = O.convlv(x, r, 1)
+    assert st == 0
+    check(got, ref, 20, form, "convlv C2")
+
+
+def test_convlv_golden(nr):
+    g = np.load(GOLD)
+    got = nr.convlv(g["convlv_1024_data"], g["convlv_1024_resp"], 1)
+    assert_fp64_close(got, g["convlv_1024_out"], 10, "golden convlv")
+    got = nr.convlv(g["convlv_1024_data"], g["convlv_1024_taps"], 1)
+    assert_fp64_close(got, g["convlv_1024_out"], 10, "golden convlv taps")
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("n", [1, 2, 4, 31, 32, 64, 1024, 1 << 20])
+def test_correl(nr, form, n):
+    a, b = W.normal(n + 3, n), W.normal(n + 4, n)
+    got = nr.correl(a, b, form=form)
+    st, ref = O.correl(a, b)
+    assert st == 0
+    check(got, ref, max(1, n.bit_length() - 1), form, "correl n=%d" % n)
+
+
+def test_correl_kats(nr):
+    # src/Correlation.rs:406-418,464-478,493-502 (direct branch, n <= 32)
+    r = nr.correl([1.0, 2.0, 3.0, 4.0], [1.0, 2.0, 3.0, 4.0])
+    assert abs(r[0] - 30.0) < 1e-10 and r[0] > r[1]
+    assert np.allclose(nr.correl([1.0, 2.0], [1.0, 2.0]), [5.0, 2.0], atol=1e-10)
+    res = nr.correl_batch([([1.0, 2.0], [1.0, 2.0]), ([3.0, 4.0], [3.0, 4.0])])
+    assert abs(res[0][0] - 5.0) < 1e-10 and abs(res[1][0] - 25.0) < 1e-10
+
+
+def test_correl_golden(nr):
+    g = np.load(GOLD)
+    got = nr.correl(g["convlv_1024_data"], g["correl_1024_b"])
+    assert_fp64_close(got, g["correl_1024_out"], 10, "golden correl")
+
+
+def test_spectra(nr):
+    x = W.normal(9, 2048)
+    m = nr.magnitude_spectrum(x)
+    p = nr.power_spectrum(x)
+    assert_fp64_close(m, O.magnitude_spectrum(x), 10, "magnitude")
+    assert_fp64_close(p, O.power_spectrum(x), 10, "power")
+
+
+def test_large_roundtrip_properties(nr):
+    # size-independent checks at a large size: round trip and Parseval
+    nn = 1 << 24
+    x = W.normal(77, 2 * nn)
+    d = x.copy()
+    nr.four1(d, nn, 1)
+    e_t = float(np.dot(x, x))
+    e_f = float(np.dot(d, d)) / nn
+    assert abs(e_f - e_t) / e_t < 1e-12
+    nr.four1(d, nn, -1)
+    d /= nn
+    assert rel_l2(d, x) < 1e-13
+
+
+def test_repeat_calls_bit_identical(nr):
+    x = W.normal(5, 1 << 16)
+    a, b = x.copy(), x.copy()
+    nr.four1(a, 1 << 15, 1)
+    nr.four1(b, 1 << 15, 1)
+    assert np.array_equal(a, b)

@@ -1,0 +1,254 @@
+"""CPU tests of the oracle: numpy/scipy agreement, the reference crate's own
+known answers, and the committed golden fixtures."""
+import os
+
+import numpy as np
+import pytest
+import scipy.fft as sf
+
+import oracle as O
+from numrs_gb300 import workloads as W
+from conftest import rel_l2
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "golden.npz")
+
+
+def cplx(d):
+    return d[0::2] + 1j * d[1::2]
+
+
+@pytest.mark.parametrize("nn", [1, 2, 4, 8, 16, 512, 1024, 2048, 4096, 1 << 14])
+@pytest.mark.parametrize("isign", [1, -1])
+def test_four1_matches_numpy(nn, isign):
+    x = W.uniform_pm1(nn + (isign > 0), 2 * nn)
+    d = x.copy()
+    O.four1(d, nn, isign)
+    z = cplx(x)
+    ref = nn * np.fft.ifft(z) if isign == 1 else np.fft.fft(z)
+    assert rel_l2(cplx(d), ref) < 1e-14
+
+
+def test_four1_hybrid_vs_recurrence():
+    # FFT_1.rs:5 (table twiddles for mmax >= 1024) vs :110 (recurrence only)
+    nn = 1 << 16
+    x = W.normal(3, 2 * nn)
+    a, b = x.copy(), x.copy()
+    O.four1(a, nn, 1)
+    O.four1_optimized(b, nn, 1)
+    assert 0 < rel_l2(a, b) < 1e-13
+
+
+def test_four1_loops_bounded_by_len():
+    # src/FFT_1.rs:52-56 bounds the butterfly loops by data.len(), not 2*nn:
+    # a longer buffer butterflies its tail (src/FFT_2.rs:452-461 passes 18 doubles)
+    d = np.array([1.0, 0.0] * 8 + [0.0, 0.0])
+    O.four1(d, 8, 1)
+    assert d.size == 18
+
+
+def test_four1_kat_roundtrip():
+    # src/FFT_1.rs:245-267: 1024-point round trip scaled by 1/N within 1e-10
+    t = np.arange(1024) / 1024.0
+    sig = np.sin(2 * np.pi * 5 * t) + 0.5 * np.cos(2 * np.pi * 20 * t)
+    c = np.zeros(2048)
+    c[0::2] = sig
+    O.four1(c, 1024, 1)
+    O.four1(c, 1024, -1)
+    c /= 1024
+    assert np.abs(c[0::2] - sig).max() < 1e-10
+
+
+def test_power_spectrum_kat():
+    # src/FFT_1.rs:304-321: |X|^2 == power spectrum
+    t = np.arange(1024) / 1024.0
+    sig = np.sin(2 * np.pi * 5 * t) + 0.5 * np.cos(2 * np.pi * 20 * t)
+    c = np.zeros(2048)
+    c[0::2] = sig
+    O.four1(c, 1024, 1)
+    m = O.magnitude_spectrum(c)
+    p = O.power_spectrum(c)
+    assert m.size == 1024 and p.size == 1024
+    assert np.abs(m * m - p).max() < 1e-10
+
+
+def test_fft_batch_matches_single():
+    sizes = [64, 512, 1024, 128]
+    arrs = [W.normal(10 + i, 2 * s) for i, s in enumerate(sizes)]
+    ref = []
+    for a, s in zip(arrs, sizes):
+        d = a.copy()
+        (O.four1_optimized if s >= 512 else O.four1)(d, s, 1)
+        ref.append(d)
+    work = [a.copy() for a in arrs]
+    O.set_threads(4)
+    O.fft_batch(work, 1)
+    O.set_threads(1)
+    for w, r in zip(work, ref):
+        assert np.array_equal(w, r)
+
+
+@pytest.mark.parametrize("n", [2, 4, 8, 256, 2048, 1 << 16])
+def test_realft_matches_numpy(n):
+    x = W.normal(n, n)
+    d = x.copy()
+    O.realft(d, n, 1)
+    X = np.conj(np.fft.rfft(x))
+    pk = np.empty(n)
+    pk[0], pk[1] = X[0].real, X[n // 2].real
+    pk[2::2], pk[3::2] = X[1:n // 2].real, X[1:n // 2].imag
+    assert rel_l2(d, pk) < 1e-14
+    O.realft(d, n, -1)
+    # Real_FT.rs:500-521 round trip, with the contract's 2/n scale
+    assert np.abs(d * 2.0 / n - x).max() < 1e-12
+
+
+def test_twofft_matches_numpy():
+    n = 256
+    a, b = W.normal(1, n), W.normal(2, n)
+    f1, f2 = O.twofft(a, b)
+    assert f1.size == 2 * n + 2
+    assert rel_l2(cplx(f1[:2 * n]), n * np.fft.ifft(a)) < 1e-14
+    assert rel_l2(cplx(f2[:2 * n]), n * np.fft.ifft(b)) < 1e-14
+    # src/FFT_2.rs:416-417: imaginary parts of the DC bins are zero
+    assert f1[1] == 0.0 and f2[1] == 0.0
+
+
+def test_fourn_matches_numpy_and_validates():
+    nn = (4, 8, 16)
+    x = W.uniform_pm1(5, 2 * int(np.prod(nn)))
+    d = x.copy()
+    assert O.fourn(d, nn, 1) == 0
+    assert rel_l2(cplx(d).reshape(nn), np.prod(nn) * np.fft.ifftn(cplx(x).reshape(nn))) < 1e-14
+    # validate_inputs (src/Fourn.rs:367-378, tests :466-476)
+    assert O.fourn(x.copy(), (1,), 1) == -1
+    assert O.fourn(x.copy(), (8,), 0) == -1
+    assert O.fourn(x.copy(), (8, 8), 1, ndim=3) == -1
+    assert O.fourn(x.copy(), (8, 8), 1, ndim=0) == -1
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 8), (4, 8, 16), (2, 4, 2), (1, 1, 8)])
+def test_rlft3_matches_numpy(shape):
+    n1, n2, n3 = shape
+    x = W.plane_waves(shape, count=4)
+    d = x.ravel().copy()
+    sp = np.zeros(n1 * 2 * n2)
+    O.rlft3(d, sp, n1, n2, n3, 1)
+    H = np.conj(np.fft.rfftn(x))
+    assert rel_l2(cplx(d).reshape(n1, n2, n3 // 2), H[:, :, :n3 // 2]) < 1e-14
+    assert rel_l2(cplx(sp).reshape(n1, n2), H[:, :, n3 // 2]) < 1e-14
+    O.rlft3(d, sp, n1, n2, n3, -1)
+    # Real_FT3.rs:267-311 round trip with the contract's 2/N scale
+    assert np.abs(d.reshape(shape) * 2.0 / (n1 * n2 * n3) - x).max() < 1e-12
+
+
+@pytest.mark.parametrize("n", [4, 8, 64, 1024])
+def test_sine_cosine_transforms(n):
+    y = W.normal(n, n)
+    y[0] = 0
+    d = y.copy()
+    O.sinft(d, n)
+    ref = np.zeros(n)
+    ref[1:] = sf.dst(y[1:], type=1) / 2
+    assert rel_l2(d, ref) < 1e-13
+    yc = W.normal(n + 1, n + 1)
+    d = yc.copy()
+    O.cosft1(d, n)
+    assert rel_l2(d, sf.dct(yc, type=1) / 2) < 1e-13
+    y2 = W.normal(n + 2, n)
+    d = y2.copy()
+    O.cosft2(d, n, 1)
+    assert rel_l2(d, sf.dct(y2, type=2) / 2) < 1e-13
+    O.cosft2(d, n, -1)
+    assert np.abs(d * 2.0 / n - y2).max() < 1e-12
+    # Cos_FT2.rs:265-271: isign other than +-1 is rejected
+    assert O.cosft2(y2.copy(), n, 0) == -1
+
+
+def _circ_conv(x, h):
+    return np.real(np.fft.ifft(np.fft.fft(x) * np.fft.fft(h)))
+
+
+@pytest.mark.parametrize("n,m", [(16, 5), (1024, 257), (4096, 3), (64, 64), (8, 1), (32, 4)])
+def test_convlv(n, m):
+    x = W.normal(n, n)
+    r = W.normal(m + 7, m)
+    st, a = O.convlv(x, r, 1)
+    assert st == 0
+    h = np.zeros(n)
+    half = (m - 1) // 2
+    h[:(m + 1) // 2] = r[:(m + 1) // 2]
+    for k in range(1, half + 1):
+        h[n - k] = r[m - k]
+    if m == n:
+        h = r.copy()
+        h[n // 2] = 0.0
+    assert rel_l2(a, _circ_conv(x, h)) < 1e-13
+    st, b = O.convlv(a, r, -1)
+    assert st == 0 and rel_l2(b, x) < 1e-12
+
+
+def test_convlv_error_order():
+    # src/Convolve.rs:405-424 and the check order at :13-21
+    assert O.convlv([], [1.0], 1)[0] == 1
+    assert O.convlv([1.0, 2.0], [1.0, 2.0, 3.0], 1)[0] == 2
+    assert O.convlv([1.0, 2.0], [1.0], 0)[0] == 3
+    assert O.convlv([1.0, 2.0, 3.0], [1.0], 1)[0] == 4  # n not a power of two
+
+
+def test_correl_kats_and_circular():
+    # small-n direct branch, src/Correlation.rs:406-418,464-478,493-502
+    st, r = O.correl([1, 2, 3, 4], [1, 2, 3, 4])
+    assert st == 0 and abs(r[0] - 30.0) < 1e-10 and r[0] > r[1]
+    assert np.allclose(O.correl([1, 2], [1, 2])[1], [5.0, 2.0])
+    assert abs(O.correl([3, 4], [3, 4])[1][0] - 25.0) < 1e-10
+    # error handling, src/Correlation.rs:452-462
+    assert O.correl([], [1.0])[0] == 1
+    assert O.correl([1.0, 2.0], [1.0])[0] == 2
+    for n in (64, 1024):
+        a, b = W.normal(n, n), W.normal(n + 1, n)
+        st, c = O.correl(a, b)
+        ref = np.array([np.dot(np.roll(a, -k), b) for k in range(n)])
+        assert st == 0 and rel_l2(c, ref) < 1e-13
+
+
+def test_golden_fixtures_reproduce():
+    g = np.load(GOLD)
+    d = g["four1_4096_in"].copy()
+    O.four1(d, 4096, 1)
+    assert np.array_equal(d, g["four1_4096_out_p"])
+    d = g["four1_4096_in"].copy()
+    O.four1(d, 4096, -1)
+    assert np.array_equal(d, g["four1_4096_out_m"])
+    d = g["realft_1024_in"].copy()
+    O.realft(d, 1024, 1)
+    assert np.array_equal(d, g["realft_1024_out"])
+    st, a = O.convlv(g["convlv_1024_data"], g["convlv_1024_resp"], 1)
+    assert np.array_equal(a, g["convlv_1024_out"])
+    st, c = O.correl(g["convlv_1024_data"], g["correl_1024_b"])
+    assert np.array_equal(c, g["correl_1024_out"])
+    d = g["fourn_8x16x32_in"].copy()
+    O.fourn(d, (8, 16, 32), 1)
+    assert np.array_equal(d, g["fourn_8x16x32_out"])
+    d = g["rlft3_8x8x16_in"].copy()
+    sp = np.zeros(128)
+    O.rlft3(d, sp, 8, 8, 16, 1)
+    assert np.array_equal(d, g["rlft3_8x8x16_out"]) and np.array_equal(sp, g["rlft3_8x8x16_speq"])
+    f1, f2 = O.twofft(g["twofft_256_a"], g["twofft_256_b"])
+    assert np.array_equal(f1, g["twofft_256_f1"]) and np.array_equal(f2, g["twofft_256_f2"])
+    for name, fn in (("sinft", lambda y: O.sinft(y, 64)), ("cosft1", lambda y: O.cosft1(y, 64)),
+                     ("cosft2", lambda y: O.cosft2(y, 64, 1))):
+        y = g[name + "_64_in"].copy()
+        fn(y)
+        assert np.array_equal(y, g[name + "_64_out"]), name
+
+
+def test_workload_generator_is_deterministic():
+    a = W.normal(123, 1001)
+    b = W.normal(123, 1001)
+    assert np.array_equal(a, b)
+    assert abs(a.mean()) < 0.15 and abs(a.std() - 1) < 0.1
+    u = W.uniform(7, 100000)
+    assert u.min() >= 0 and u.max() < 1 and abs(u.mean() - 0.5) < 0.01
+    sizes, u = W.batch_c3(count=2000)
+    assert sizes.min() >= 64 and sizes.max() <= 1 << 14
+    assert len(set(sizes.tolist())) == 9
