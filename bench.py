@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--form", default="fp64", choices=["fp64", "df64", "fp32"])
     ap.add_argument("--no-forms", action="store_true", help="skip the extra precision forms")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--log2n", type=int, default=0, help="four1 workload size (default 2^24)")
     return ap.parse_args()
 
 
@@ -386,6 +387,77 @@ def run_convlv(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_four1(args, world, rank, local):
+    """One in-place complex FFT of 2^log2n points per step (device resident)."""
+    import torch
+    import numrs_gb300 as nr
+    from numrs_gb300 import workloads as W
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    log2n = args.log2n or (28 if args.workload == "large" else 24)
+    nn = 1 << log2n
+    x = W.normal(W.BASE_SEED + 5, 2 * nn) if log2n <= 24 else None
+    d = torch.from_numpy(x).to(dev) if x is not None else torch.randn(2 * nn, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    nr.set_async(True)
+    sign = [1]
+
+    def step():
+        nr.four1(d, nn, sign[0], form=args.form)
+        sign[0] = -sign[0]
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    nr.launch_count(reset=True)
+    for i in range(args.steps):
+        if nn * 16 < (256 << 20):
+            flush.zero_()
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    launches = nr.launch_count()
+    clk = clocks.stop()
+    total_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), world)
+    flops = 5.0 * nn * log2n
+    nr.profile(True)
+    for i in range(min(args.steps, 20)):
+        step()
+    torch.cuda.synchronize()
+    pass_ms, pass_n, pass_bytes, pass_flops = nr.profile_read("pass")
+    nr.profile(False)
+    nr.set_async(False)
+    if rank != 0:
+        return None
+    hbm, hbm_kind = peaks()
+    achieved = pass_bytes / (pass_ms / 1e3) / 1e9 if pass_ms else 0.0
+    return {
+        "metric": METRIC, "value": flops * args.steps * world / (total_ms / 1e3) / 1e9,
+        "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.form == "fp64" else args.form,
+        "data": "synthetic N(0,1) complex",
+        "config": {"workload": "four1 complex in-place FFT, N=2^%d (%d MiB), alternating isign"
+                               % (log2n, (16 * nn) >> 20), "form": args.form,
+                   "l2": "input larger than L2" if nn * 16 >= (256 << 20) else "flushed between steps"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "kernel": "k_pass (Stockham pass)",
+                     "launches": pass_n, "avg_launch_ms": pass_ms / max(pass_n, 1),
+                     "bytes_per_launch": pass_bytes / max(pass_n, 1)},
+        "compute_roofline": {"bound": "fp64" if args.form == "fp64" else "fp32",
+                             "achieved_tflops": pass_flops / (pass_ms / 1e3) / 1e12 if pass_ms else 0.0,
+                             "peak_tflops": FP64_PEAK_TFLOPS if args.form == "fp64" else 73.3},
+        "clocks": clk, "gpu_launches": launches,
+    }
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -397,7 +469,11 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    if args.workload != "convlv":
+    if args.workload in ("four1", "large"):
+        line = run_four1(args, world, rank, local)
+        if line:
+            print(json.dumps(line), flush=True)
+    elif args.workload != "convlv":
         raise SystemExit("workload %s is not wired into bench.py yet" % args.workload)
     else:
         run_convlv(args, world, rank, local)

@@ -207,20 +207,43 @@ __device__ __forceinline__ void gstore(void* p, long long i, typename F::C a) {
 }
 
 // ---------------------------------------------------------------------------
-// The pass kernel.  T threads, tile of 16*T complex elements.
+// One tile of one pass (T threads, 16*T complex elements).  Used by the
+// per-pass kernel (one tile per CTA) and by the persistent batch kernel.
+// L2_ONLY loads bypass L1 (data written by other CTAs of the same launch).
 // ---------------------------------------------------------------------------
-template <class F, int SG, int IN, int OUT, int T>
-__global__ void __launch_bounds__(T) k_pass(PassParams p) {
+template <int IO>
+struct IOElem;
+template <> struct IOElem<IO_D2> { using T = d2; };
+template <> struct IOElem<IO_F2> { using T = f2; };
+template <> struct IOElem<IO_F4> { using T = f4; };
+
+template <class F, int IO, bool L2_ONLY>
+__device__ __forceinline__ typename F::C gload_elem(const void* base, long long i) {
+  using E = typename IOElem<IO>::T;
+  const E* p = reinterpret_cast<const E*>(base) + i;
+  if constexpr (L2_ONLY) {
+    if constexpr (IO == IO_F2) {
+      float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+      return gload<F, IO>(&v, 0);
+    } else {
+      float4 v = __ldcg(reinterpret_cast<const float4*>(p));
+      return gload<F, IO>(&v, 0);
+    }
+  } else {
+    return gload<F, IO>(p, 0);
+  }
+}
+
+template <class F, int SG, int IN, int OUT, int T, bool L2_ONLY>
+__device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
+                                          typename F::S* sm, int tid) {
   using C = typename F::C;
-  using S = typename F::S;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  S* sm = reinterpret_cast<S*>(smem_raw);
+  using IE = typename IOElem<IN>::T;
+  using OE = typename IOElem<OUT>::T;
   constexpr int sh = F::kPadShift;
-  const int tid = threadIdx.x;
   const int logR = p.logR, logC = p.logC;
   const int R = 1 << logR;
   const int Cn = 1 << logC;
-  const long long tile = blockIdx.x;
 
   // tile -> (first line, first j)
   long long line0, j0;
@@ -247,9 +270,10 @@ __global__ void __launch_bounds__(T) k_pass(PassParams p) {
     if (p.mode == 0) j += c; else line += c;
     C v;
     if (line < p.nlines) {
-      const long long base = (line >> p.lq_log) * p.lstride + (line & lqmask);
-      const long long idx = base + (j + ((long long)r << logLR)) * p.s;
-      v = gload<F, IN>(p.in, idx);
+      const IE* base = p.in_ptrs
+          ? reinterpret_cast<const IE*>(p.in_ptrs[line])
+          : reinterpret_cast<const IE*>(p.in) + ((line >> p.lq_log) * p.lstride + (line & lqmask));
+      v = gload_elem<F, IN, L2_ONLY>(base, (j + ((long long)r << logLR)) * p.s);
       if (p.logNs > 0) {
         const long long jm = j & (p.Ns - 1);
         if (jm != 0 && r != 0) v = F::mul(v, twiddle<F>(p.tw, p.logNs + logR, jm * r, SG));
@@ -286,11 +310,20 @@ __global__ void __launch_bounds__(T) k_pass(PassParams p) {
     if (line >= p.nlines) continue;
     C v = F::from_s(sm[pidx((c << logR) + r, sh)]);
     if (p.do_scale) v = F::scale(v, p.scale);
-    const long long base = (line >> p.lq_log) * p.lstride + (line & lqmask);
+    OE* base = p.out_ptrs
+        ? reinterpret_cast<OE*>(p.out_ptrs[line])
+        : reinterpret_cast<OE*>(p.out) + ((line >> p.lq_log) * p.lstride + (line & lqmask));
     const long long jd = ((j >> p.logNs) << (p.logNs + logR)) + (j & (p.Ns - 1));
-    const long long idx = base + (jd + ((long long)r << p.logNs)) * p.s;
-    gstore<F, OUT>(p.out, idx, v);
+    gstore<F, OUT>(base, (jd + ((long long)r << p.logNs)) * p.s, v);
   }
+}
+
+// One CTA per tile.
+template <class F, int SG, int IN, int OUT, int T>
+__global__ void __launch_bounds__(T) k_pass(PassParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  pass_tile<F, SG, IN, OUT, T, false>(p, blockIdx.x, reinterpret_cast<typename F::S*>(smem_raw),
+                                      threadIdx.x);
 }
 
 template <class F>
@@ -299,46 +332,30 @@ inline size_t pass_smem_bytes(int T) {
   return sizeof(typename F::S) * (size_t)(E + (E >> F::kPadShift));
 }
 
-template <class K>
-inline void set_smem_once(K k, size_t smem) {
-  static size_t done = 0;  // one static per kernel instantiation
-  if (done < smem) {
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    done = smem;
+// Launch one k_pass instantiation; its dynamic shared memory limit is raised
+// once per instantiation (the static lives in this function template).
+template <class F, int SG, int IN, int OUT, int T>
+inline cudaError_t launch_pass_one(const PassParams& p, cudaStream_t st) {
+  static size_t attr_done = 0;
+  const size_t smem = pass_smem_bytes<F>(T);
+  if (attr_done < smem) {
+    cudaError_t e = cudaFuncSetAttribute(k_pass<F, SG, IN, OUT, T>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_done = smem;
   }
+  k_pass<F, SG, IN, OUT, T><<<dim3((unsigned)p.tiles), T, smem, st>>>(p);
+  return cudaGetLastError();
 }
 
 template <class F, int SG, int IN, int OUT>
 cudaError_t launch_pass_t(const PassParams& p, int threads, cudaStream_t st) {
-  const size_t smem = pass_smem_bytes<F>(threads);
-  dim3 grid((unsigned)p.tiles);
   switch (threads) {
-    case 256: {
-      auto k = k_pass<F, SG, IN, OUT, 256>;
-      set_smem_once(k, smem);
-      k<<<grid, 256, smem, st>>>(p);
-      break;
-    }
-    case 128: {
-      auto k = k_pass<F, SG, IN, OUT, 128>;
-      set_smem_once(k, smem);
-      k<<<grid, 128, smem, st>>>(p);
-      break;
-    }
-    case 64: {
-      auto k = k_pass<F, SG, IN, OUT, 64>;
-      set_smem_once(k, smem);
-      k<<<grid, 64, smem, st>>>(p);
-      break;
-    }
-    default: {
-      auto k = k_pass<F, SG, IN, OUT, 32>;
-      set_smem_once(k, smem);
-      k<<<grid, 32, smem, st>>>(p);
-      break;
-    }
+    case 256: return launch_pass_one<F, SG, IN, OUT, 256>(p, st);
+    case 128: return launch_pass_one<F, SG, IN, OUT, 128>(p, st);
+    case 64: return launch_pass_one<F, SG, IN, OUT, 64>(p, st);
+    default: return launch_pass_one<F, SG, IN, OUT, 32>(p, st);
   }
-  return cudaGetLastError();
 }
 
 }  // namespace gbfft

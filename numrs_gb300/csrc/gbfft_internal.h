@@ -46,6 +46,10 @@ struct Twiddles {
 struct PassParams {
   const void* in;
   void* out;
+  // optional per-line base pointers (complex elements of the IO type); when
+  // set they replace in/out + the line offset (lines are separate arrays)
+  const void* const* in_ptrs;
+  void* const* out_ptrs;
   Twiddles tw;
   long long L;
   long long s;
@@ -115,6 +119,10 @@ cudaError_t launch_cosft1_pre(double* y, long long n, double* partial, Twiddles 
                               cudaStream_t st);
 cudaError_t launch_cosft2_pre(int isign, double* y, long long n, Twiddles tw, cudaStream_t st);
 cudaError_t launch_cosft2_rot(int isign, double* y, long long n, Twiddles tw, cudaStream_t st);
+cudaError_t launch_cosft2_inv_pre(const double* y, double* w, long long n, Twiddles tw,
+                                  cudaStream_t st);
+cudaError_t launch_cosft2_inv_post(const double* w, double* y, long long n, Twiddles tw,
+                                   cudaStream_t st);
 // Ordered prefix sums on the odd/even slots after realft (sinft/cosft1/cosft2).
 cudaError_t launch_trig_scan(int kind, double* y, long long n, double* partial, double* work,
                              cudaStream_t st);

@@ -217,6 +217,8 @@ AxisPlan make_axis_plan(long long L, long long s, long long nlines, int lq_log,
     PassParams& p = ps.p;
     std::memset(&p, 0, sizeof p);
     const int logR = radix[i];
+    p.in_ptrs = nullptr;
+    p.out_ptrs = nullptr;
     p.L = L;
     p.s = s;
     p.lstride = lstride;
@@ -875,17 +877,101 @@ int gbfft_power_spectrum(const double* c, size_t nn, double* out, const gbfft_op
   return spectrum_call(1, c, nn, out, opts);
 }
 
+static int trig_check(const Call& c, double* y, size_t n, const char* what) {
+  TRY(check_form(c));
+  if (!y) return fail(GBFFT_INVALID_ARG, "%s: null data", what);
+  if (n < 2 || !is_pow2(n) || ilog2(n) > kMaxAxisLog - 2)
+    return fail(GBFFT_UNSUPPORTED_SIZE, "%s: n=%zu must be a power of two >= 2", what, n);
+  return GBFFT_OK;
+}
+
+// work area for the trig scans: n/2 values, chunk totals, a few scalars, and
+// the per-block partial sums of cosft1
+static int trig_work(size_t n, double** work, double** partial) {
+  const size_t M = n / 2;
+  const size_t chunks = (M + 2047) / 2048;
+  const size_t np = 152 * 16 + 1;
+  TRY(ensure(g.work, (M + chunks + 2 + np + 8) * sizeof(double)));
+  *work = (double*)g.work.p;
+  *partial = *work + M + chunks + 4;
+  return GBFFT_OK;
+}
+
 int gbfft_sinft(double* y, size_t n, const gbfft_opts* opts) {
-  (void)y; (void)n; (void)opts;
-  return fail(GBFFT_UNSUPPORTED_SIZE, "sinft: not built yet");
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(trig_check(c, y, n, "sinft"));
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  Twiddles tw;
+  TRY(tables(FORM_F64, tw));
+  double* d;
+  TRY(stage_inout(c, g.stage_a, y, n, &d));
+  double *work, *partial;
+  TRY(trig_work(n, &work, &partial));
+  CK(launch_sinft_pre(d, (long long)n, tw, g.cur));
+  g.launches++;
+  TRY(realft_dev(c.form(), d, (long long)n, 1));
+  CK(launch_trig_scan(0, d, (long long)n, nullptr, work, g.cur));
+  g.launches += 3;
+  TRY(unstage(c, y, d, n));
+  return ss.finish(c);
 }
+
 int gbfft_cosft1(double* y, size_t n, const gbfft_opts* opts) {
-  (void)y; (void)n; (void)opts;
-  return fail(GBFFT_UNSUPPORTED_SIZE, "cosft1: not built yet");
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(trig_check(c, y, n, "cosft1"));
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  Twiddles tw;
+  TRY(tables(FORM_F64, tw));
+  double* d;
+  TRY(stage_inout(c, g.stage_a, y, n + 1, &d));
+  double *work, *partial;
+  TRY(trig_work(n, &work, &partial));
+  CK(launch_cosft1_pre(d, (long long)n, partial, tw, g.cur));
+  g.launches += 2;
+  TRY(realft_dev(c.form(), d, (long long)n, 1));
+  CK(launch_trig_scan(1, d, (long long)n, partial, work, g.cur));
+  g.launches += 3;
+  TRY(unstage(c, y, d, n + 1));
+  return ss.finish(c);
 }
+
 int gbfft_cosft2(double* y, size_t n, int isign, const gbfft_opts* opts) {
-  (void)y; (void)n; (void)isign; (void)opts;
-  return fail(GBFFT_UNSUPPORTED_SIZE, "cosft2: not built yet");
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(trig_check(c, y, n, "cosft2"));
+  // src/Cos_FT2.rs:8-12 panics on any other isign
+  if (isign != 1 && isign != -1) return fail(GBFFT_INVALID_ARG, "Invalid isign value: %d. Must be 1 or -1", isign);
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  Twiddles tw;
+  TRY(tables(FORM_F64, tw));
+  double* d;
+  TRY(stage_inout(c, g.stage_a, y, n, &d));
+  double *work, *partial;
+  TRY(trig_work(n, &work, &partial));
+  if (isign == 1) {
+    CK(launch_cosft2_pre(1, d, (long long)n, tw, g.cur));
+    g.launches++;
+    TRY(realft_dev(c.form(), d, (long long)n, 1));
+    CK(launch_cosft2_rot(1, d, (long long)n, tw, g.cur));
+    g.launches++;
+    CK(launch_trig_scan(2, d, (long long)n, nullptr, work, g.cur));
+    g.launches += 3;
+  } else {
+    TRY(ensure(g.stage_c, n * sizeof(double)));
+    double* w = (double*)g.stage_c.p;
+    CK(launch_cosft2_inv_pre(d, w, (long long)n, tw, g.cur));
+    g.launches++;
+    TRY(realft_dev(c.form(), w, (long long)n, -1));
+    CK(launch_cosft2_inv_post(w, d, (long long)n, tw, g.cur));
+    g.launches++;
+  }
+  TRY(unstage(c, y, d, n));
+  return ss.finish(c);
 }
 
 }  // extern "C"

@@ -263,6 +263,40 @@ def test_correl_golden(nr):
     assert_fp64_close(got, g["correl_1024_out"], 10, "golden correl")
 
 
+@pytest.mark.parametrize("form", ["fp64", "df64"])
+@pytest.mark.parametrize("n", [2, 4, 8, 64, 1024, 1 << 16, 1 << 20])
+def test_sine_cosine_transforms(nr, form, n):
+    log2n = n.bit_length() - 1
+    y = W.normal(n + 5, n)
+    d, ref = y.copy(), y.copy()
+    nr.sinft(d, n, form=form)
+    O.sinft(ref, n)
+    check(d, ref, log2n, form, "sinft n=%d" % n)
+    yc = W.normal(n + 6, n + 1)
+    d, ref = yc.copy(), yc.copy()
+    nr.cosft1(d, n, form=form)
+    O.cosft1(ref, n)
+    check(d, ref, log2n, form, "cosft1 n=%d" % n)
+    y2 = W.normal(n + 7, n)
+    for isign in (1, -1):
+        d, ref = y2.copy(), y2.copy()
+        nr.cosft2(d, n, isign, form=form)
+        O.cosft2(ref, n, isign)
+        check(d, ref, log2n, form, "cosft2 n=%d isign=%d" % (n, isign))
+
+
+def test_sine_cosine_golden(nr):
+    g = np.load(GOLD)
+    for name, fn in (("sinft", lambda y: nr.sinft(y, 64)), ("cosft1", lambda y: nr.cosft1(y, 64)),
+                     ("cosft2", lambda y: nr.cosft2(y, 64, 1))):
+        y = g[name + "_64_in"].copy()
+        fn(y)
+        assert_fp64_close(y, g[name + "_64_out"], 6, "golden " + name)
+    y = g["cosft2_64_in"].copy()
+    nr.cosft2(y, 64, -1)
+    assert_fp64_close(y, g["cosft2_64_inv_out"], 6, "golden cosft2 inverse")
+
+
 def test_spectra(nr):
     x = W.normal(9, 2048)
     m = nr.magnitude_spectrum(x)
