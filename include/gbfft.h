@@ -15,8 +15,8 @@
  *
  * Every function returns a gbfft_status.  Pointers are host memory unless
  * opts->device_ptrs is set.  Calls are synchronous for host pointers; for
- * device pointers they are ordered on opts->stream (or the library stream)
- * and synchronous unless opts->async is set.  The library is thread-safe
+ * device pointers they are ordered on opts->stream (NULL = the default
+ * stream) and synchronous unless opts->async is set.  The library is thread-safe
  * (one internal lock).  No entry point changes any GPU setting.
  */
 #ifndef GBFFT_H
@@ -54,7 +54,7 @@ typedef enum {
 typedef struct {
   int form;          /* gbfft_form; 0 = FP64                                   */
   int device_ptrs;   /* 1: all array arguments are device pointers             */
-  void* stream;      /* cudaStream_t for device-pointer calls, NULL = library  */
+  void* stream;      /* cudaStream_t of device-pointer calls, NULL = default   */
   int async;         /* device-pointer calls only: 1 = do not synchronise      */
 } gbfft_opts;
 

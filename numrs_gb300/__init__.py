@@ -33,6 +33,7 @@ __all__ = [
     "cosft1", "cosft2", "sinft", "convlv", "correl", "convlv_batch", "correl_batch",
     "autocorrel", "magnitude_spectrum", "power_spectrum", "real_to_complex",
     "complex_to_real", "ConvlvError", "CorrelError", "GbfftError", "launch_count",
+    "FFTBatch", "four1_many", "set_async", "profile", "profile_read",
 ]
 
 
@@ -207,6 +208,28 @@ class FFTProcessor:
         ptrs = (ctypes.c_void_p * n)(*[x.ptr for x in args])
         nns = (ctypes.c_size_t * n)(*[x.size // 2 for x in args])
         _check(_lib.load().gbfft_four1_batch(ptrs, nns, n, isign, ctypes.byref(o)))
+
+
+class FFTBatch:
+    """A fixed list of arrays transformed together, the marshalling done once.
+
+    ``FFTBatch(arrays).run(isign)`` is ``FFTProcessor().fft_batch(arrays, isign)``
+    without rebuilding the pointer tables; the library caches the device plan
+    and a CUDA graph of it, so repeated runs on the same device tensors are one
+    graph launch each.
+    """
+
+    def __init__(self, arrays, form="fp64"):
+        self.args = [_Arg(a, True) for a in arrays]
+        self.form = form
+        n = len(self.args)
+        self.n = n
+        self.ptrs = (ctypes.c_void_p * n)(*[x.ptr for x in self.args])
+        self.nns = (ctypes.c_size_t * n)(*[x.size // 2 for x in self.args])
+
+    def run(self, isign):
+        o = _opts(self.args, self.form)
+        _check(_lib.load().gbfft_four1_batch(self.ptrs, self.nns, self.n, isign, ctypes.byref(o)))
 
 
 def twofft(data1, data2, fft1, fft2, form="fp64"):

@@ -1,0 +1,36 @@
+// batch.h -- descriptors of the persistent batched FFT launch (batch.cu).
+#pragma once
+#include "gbfft_internal.h"
+
+namespace gbfft {
+
+// One pass of one size bin: a contiguous run of queue items.
+//   kind 0  single-pass bin: caller arrays -> caller arrays
+//   kind 1  pass 1 of a two-pass bin: caller arrays -> bin scratch; each tile
+//           bumps done[first + line] when its stores are visible
+//   kind 2  pass 2: bin scratch -> caller arrays; each tile first waits until
+//           done[first + line] == need
+struct BatchRange {
+  PassParams p;
+  long long item0;
+  long long first;
+  unsigned int need;
+  int kind;
+};
+
+struct BatchParams {
+  const BatchRange* ranges;  // device copy, sorted by item0
+  int nranges;
+  long long total;           // queue length
+  unsigned long long* head;  // next queue item (zeroed before the launch)
+  unsigned int* done;        // per-transform pass-1 tile counters (zeroed)
+  int* err;                  // set to 1 when a bounded wait gives up (zeroed)
+  unsigned int spin_limit;
+};
+
+cudaError_t launch_batch(Form f, int sign, const BatchParams& P, int grid, cudaStream_t st);
+// Resident CTAs per SM; also raises the kernel's shared memory limit, so it
+// is called before the launch is captured.
+int batch_blocks_per_sm(Form f, int sign);
+
+}  // namespace gbfft

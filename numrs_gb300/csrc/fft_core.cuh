@@ -318,9 +318,10 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
   }
 }
 
-// One CTA per tile.
+// One CTA per tile.  Two 256-thread CTAs fit on an SM (registers capped at
+// 128, shared memory 2 x 70 KB), which covers the FP64 pipe's latency.
 template <class F, int SG, int IN, int OUT, int T>
-__global__ void __launch_bounds__(T) k_pass(PassParams p) {
+__global__ void __launch_bounds__(T, (T == 256 ? 2 : 1)) k_pass(PassParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   pass_tile<F, SG, IN, OUT, T, false>(p, blockIdx.x, reinterpret_cast<typename F::S*>(smem_raw),
                                       threadIdx.x);

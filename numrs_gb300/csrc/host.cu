@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/gbfft.h"
+#include "batch.h"
 #include "gbfft_internal.h"
 
 namespace gbfft {
@@ -199,7 +200,7 @@ void split_subpasses(int logR, PassParams& p) {
 }
 
 AxisPlan make_axis_plan(long long L, long long s, long long nlines, int lq_log,
-                        long long lstride) {
+                        long long lstride, bool full_tile = false) {
   AxisPlan ap;
   const int logL = ilog2((unsigned long long)L);
   std::vector<int> radix;
@@ -239,7 +240,7 @@ AxisPlan make_axis_plan(long long L, long long s, long long nlines, int lq_log,
       p.mode = 1;
       int want = ilog2(kTileE) - logR;
       int have = ilog2(npow2((unsigned long long)nlines));
-      logC = std::min(want, have);
+      logC = full_tile ? want : std::min(want, have);
       p.in_rcontig = (s == 1) ? 1 : 0;
       p.out_rcontig = (s == 1) ? 1 : 0;
     }
@@ -350,11 +351,12 @@ int check_form(const Call& c) {
   return GBFFT_OK;
 }
 
-// Stream handling: a device-pointer call that names a stream runs on it;
-// every other call runs on the library stream.
+// Stream handling: a device-pointer call runs on the caller's stream (NULL is
+// the default stream, so the call is ordered after earlier default-stream
+// work); host-pointer calls run on the library stream.
 struct StreamScope {
   explicit StreamScope(const Call& c) {
-    g.cur = (c.dev() && c.o->stream) ? (cudaStream_t)c.o->stream : g.stream;
+    g.cur = c.dev() ? (cudaStream_t)c.o->stream : g.stream;
   }
   int finish(const Call& c) {
     if (!c.dev() || !c.o->async) CK(cudaStreamSynchronize(g.cur));
@@ -464,6 +466,191 @@ int spectral_dev(Form f, int kind, double* w, long long n) {
   return GBFFT_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Persistent batched FFT (uneven sizes).  The plan of the most recent call is
+// kept with an instantiated CUDA graph of [reset counters, persistent launch];
+// an identical call (same sizes, pointers, form, direction) replays it.
+// ---------------------------------------------------------------------------
+constexpr int kBatchMaxLog = 20;   // two passes at most in the persistent queue
+
+struct BatchPlan {
+  std::vector<size_t> nn;
+  std::vector<const void*> ptrs;
+  int form = -1, sign = 0;
+  DevBuf ranges, ptrtab, done, flags, scratch;
+  BatchParams P;
+  int grid = 0;
+  cudaGraphExec_t exec = nullptr;
+  long long launches_per_call = 0;
+  bool valid = false;
+};
+BatchPlan g_batch;
+
+void batch_plan_free(BatchPlan& b) {
+  if (b.exec || b.ranges.p) cudaDeviceSynchronize();  // an earlier replay may be in flight
+  if (b.exec) cudaGraphExecDestroy(b.exec);
+  b.exec = nullptr;
+  for (DevBuf* d : {&b.ranges, &b.ptrtab, &b.done, &b.flags, &b.scratch}) {
+    if (d->p) cudaFree(d->p);
+    d->p = nullptr;
+    d->bytes = 0;
+  }
+  b.valid = false;
+}
+
+int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const size_t* nn,
+                     size_t count) {
+  batch_plan_free(b);
+  b.nn.assign(nn, nn + count);
+  b.ptrs.assign((const void* const*)dptrs, (const void* const*)dptrs + count);
+  b.form = f;
+  b.sign = sign;
+  std::vector<size_t> order(count);
+  for (size_t i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t c) { return nn[a] > nn[c]; });
+  std::vector<const void*> table(count);
+  for (size_t i = 0; i < count; ++i) table[i] = dptrs[order[i]];
+  TRY(ensure(b.ptrtab, count * sizeof(void*)));
+  CK(cudaMemcpy(b.ptrtab.p, table.data(), count * sizeof(void*), cudaMemcpyHostToDevice));
+  const void* const* dtab = (const void* const*)b.ptrtab.p;
+  // bins
+  struct Bin { long long L, count, first; };
+  std::vector<Bin> bins;
+  for (size_t i = 0; i < count;) {
+    size_t j = i;
+    while (j < count && nn[order[j]] == nn[order[i]]) ++j;
+    bins.push_back({(long long)nn[order[i]], (long long)(j - i), (long long)i});
+    i = j;
+  }
+  const IOType sio = scratch_io(f);
+  size_t scratch_elems = 0;
+  for (auto& bn : bins)
+    if (bn.L > kTileE) scratch_elems += (size_t)(bn.L * bn.count);
+  if (scratch_elems) TRY(ensure(b.scratch, scratch_elems * io_bytes(sio)));
+  Twiddles tw;
+  TRY(tables(f, tw));
+  std::vector<BatchRange> first_pass, single, second_pass;
+  size_t soff = 0;
+  for (auto& bn : bins) {
+    if (bn.L == 1) continue;  // 1-point transforms are the identity
+    AxisPlan ap = make_axis_plan(bn.L, 1, bn.count, 0, bn.L, true);
+    if (ap.passes.size() == 1) {
+      BatchRange r;
+      std::memset(&r, 0, sizeof r);
+      r.p = ap.passes[0].p;
+      r.p.tw = tw;
+      r.p.in_ptrs = (const void* const*)(dtab + bn.first);
+      r.p.out_ptrs = (void* const*)(dtab + bn.first);
+      r.kind = 0;
+      r.first = bn.first;
+      single.push_back(r);
+    } else {
+      char* sbase = (char*)b.scratch.p + soff * io_bytes(sio);
+      soff += (size_t)(bn.L * bn.count);
+      BatchRange r1, r2;
+      std::memset(&r1, 0, sizeof r1);
+      std::memset(&r2, 0, sizeof r2);
+      r1.p = ap.passes[0].p;
+      r1.p.tw = tw;
+      r1.p.in_ptrs = (const void* const*)(dtab + bn.first);
+      r1.p.out = sbase;
+      r1.kind = 1;
+      r1.first = bn.first;
+      r2.p = ap.passes[1].p;
+      r2.p.tw = tw;
+      r2.p.in = sbase;
+      r2.p.out_ptrs = (void* const*)(dtab + bn.first);
+      r2.kind = 2;
+      r2.first = bn.first;
+      r2.need = (unsigned int)(r1.p.tiles / bn.count);
+      first_pass.push_back(r1);
+      second_pass.push_back(r2);
+    }
+  }
+  std::vector<BatchRange> all;
+  for (auto* v : {&first_pass, &single, &second_pass})
+    for (auto& r : *v) all.push_back(r);
+  long long item = 0;
+  for (auto& r : all) {
+    r.item0 = item;
+    item += r.p.tiles;
+  }
+  TRY(ensure(b.ranges, std::max<size_t>(all.size(), 1) * sizeof(BatchRange)));
+  if (!all.empty())
+    CK(cudaMemcpy(b.ranges.p, all.data(), all.size() * sizeof(BatchRange), cudaMemcpyHostToDevice));
+  TRY(ensure(b.done, std::max<size_t>(count, 1) * sizeof(unsigned int)));
+  TRY(ensure(b.flags, 64));
+  std::memset(&b.P, 0, sizeof b.P);
+  b.P.ranges = (const BatchRange*)b.ranges.p;
+  b.P.nranges = (int)all.size();
+  b.P.total = item;
+  b.P.head = (unsigned long long*)b.flags.p;
+  b.P.err = (int*)((char*)b.flags.p + 8);
+  b.P.done = (unsigned int*)b.done.p;
+  b.P.spin_limit = 1u << 24;
+  int dev_sms = 0;
+  CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, g.device));
+  int per = batch_blocks_per_sm(f, sign);
+  if (per < 1) per = 1;
+  b.grid = (int)std::min<long long>((long long)dev_sms * per, std::max<long long>(item, 1));
+  // capture [reset counters, persistent launch] on the library stream
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal));
+  cudaMemsetAsync(b.flags.p, 0, 16, g.stream);
+  cudaMemsetAsync(b.done.p, 0, std::max<size_t>(count, 1) * sizeof(unsigned int), g.stream);
+  cudaError_t le = cudaSuccess;
+  if (item > 0) le = launch_batch(f, sign, b.P, b.grid, g.stream);
+  cudaError_t ce = cudaStreamEndCapture(g.stream, &graph);
+  if (le != cudaSuccess || ce != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return fail(GBFFT_CUDA_ERROR, "batch graph capture: %s / %s", cudaGetErrorString(le),
+                cudaGetErrorString(ce));
+  }
+  CK(cudaGraphInstantiate(&b.exec, graph, 0));
+  cudaGraphDestroy(graph);
+  b.launches_per_call = item > 0 ? 1 : 0;
+  b.valid = true;
+  return GBFFT_OK;
+}
+
+bool batch_plan_matches(const BatchPlan& b, Form f, int sign, double* const* dptrs,
+                        const size_t* nn, size_t count) {
+  if (!b.valid || b.form != (int)f || b.sign != sign || b.nn.size() != count) return false;
+  for (size_t i = 0; i < count; ++i)
+    if (b.nn[i] != nn[i] || b.ptrs[i] != (const void*)dptrs[i]) return false;
+  return true;
+}
+
+// Transforms of at most 2^20 points go through the persistent launch; larger
+// ones (rare in a batch) run their own pass schedule.
+int run_batch_dev(Form f, int sign, double* const* dptrs, const size_t* nn, size_t count,
+                  bool check_err) {
+  std::vector<double*> small_p, big_p;
+  std::vector<size_t> small_n, big_n;
+  for (size_t i = 0; i < count; ++i) {
+    if (ilog2(nn[i]) <= kBatchMaxLog) { small_p.push_back(dptrs[i]); small_n.push_back(nn[i]); }
+    else { big_p.push_back(dptrs[i]); big_n.push_back(nn[i]); }
+  }
+  if (!small_p.empty()) {
+    if (!batch_plan_matches(g_batch, f, sign, small_p.data(), small_n.data(), small_p.size()))
+      TRY(build_batch_plan(g_batch, f, sign, small_p.data(), small_n.data(), small_p.size()));
+    {
+      ProfScope ps(PK_PASS, 0.0);
+      CK(cudaGraphLaunch(g_batch.exec, g.cur));
+    }
+    g.launches += g_batch.launches_per_call;
+    if (check_err) {
+      int err = 0;
+      CK(cudaMemcpyAsync(&err, g_batch.P.err, sizeof(int), cudaMemcpyDeviceToHost, g.cur));
+      CK(cudaStreamSynchronize(g.cur));
+      if (err) return fail(GBFFT_TIMEOUT, "four1_batch: a bounded device wait gave up");
+    }
+  }
+  for (size_t i = 0; i < big_p.size(); ++i)
+    TRY(fft_lines(f, sign, big_p[i], (long long)big_n[i], 1, (long long)big_n[i]));
+  return GBFFT_OK;
+}
+
 }  // namespace
 }  // namespace gbfft
 
@@ -498,6 +685,7 @@ int gbfft_release(void) {
     b->bytes = 0;
   }
   g_plans.clear();
+  batch_plan_free(g_batch);
   return GBFFT_OK;
 }
 
@@ -596,56 +784,33 @@ int gbfft_four1_batch(double* const* ptrs, const size_t* nn, size_t count, int i
   }
   TRY(init_locked(g.device));
   StreamScope ss(c);
-  // group by size; each group is packed contiguously and runs as one batch
-  std::map<size_t, std::vector<size_t>> groups;
-  size_t total = 0;
-  for (size_t t = 0; t < count; ++t) {
-    groups[nn[t]].push_back(t);
-    total += 2 * nn[t];
+  const bool check = !c.dev() || !c.o->async;
+  if (c.dev()) {
+    TRY(run_batch_dev(c.form(), isign, ptrs, nn, count, check));
+    return ss.finish(c);
   }
+  // host arrays: pack into one staging buffer (one copy each way)
+  size_t total = 0;
+  for (size_t t = 0; t < count; ++t) total += 2 * nn[t];
   TRY(ensure(g.stage_b, total * sizeof(double)));
   double* packed = (double*)g.stage_b.p;
-  if (!c.dev()) {
-    g.host_pack.resize(total * sizeof(double));
-    double* hp = (double*)g.host_pack.data();
-    size_t off = 0;
-    for (auto& kv : groups)
-      for (size_t t : kv.second) {
-        std::memcpy(hp + off, ptrs[t], 2 * kv.first * sizeof(double));
-        off += 2 * kv.first;
-      }
-    TRY(h2d(packed, hp, total * sizeof(double)));
-  } else {
-    size_t off = 0;
-    for (auto& kv : groups)
-      for (size_t t : kv.second) {
-        TRY(d2d(packed + off, ptrs[t], 2 * kv.first * sizeof(double)));
-        off += 2 * kv.first;
-      }
-  }
+  g.host_pack.resize(total * sizeof(double));
+  double* hp = (double*)g.host_pack.data();
+  std::vector<double*> dp(count);
   size_t off = 0;
-  for (auto& kv : groups) {
-    long long L = (long long)kv.first, cnt = (long long)kv.second.size();
-    TRY(fft_lines(c.form(), isign, packed + off, L, cnt, L));
-    off += 2 * kv.first * kv.second.size();
+  for (size_t t = 0; t < count; ++t) {
+    std::memcpy(hp + off, ptrs[t], 2 * nn[t] * sizeof(double));
+    dp[t] = packed + off;
+    off += 2 * nn[t];
   }
-  if (!c.dev()) {
-    double* hp = (double*)g.host_pack.data();
-    TRY(d2h(hp, packed, total * sizeof(double)));
-    CK(cudaStreamSynchronize(g.cur));
-    size_t o2 = 0;
-    for (auto& kv : groups)
-      for (size_t t : kv.second) {
-        std::memcpy(ptrs[t], hp + o2, 2 * kv.first * sizeof(double));
-        o2 += 2 * kv.first;
-      }
-  } else {
-    size_t o2 = 0;
-    for (auto& kv : groups)
-      for (size_t t : kv.second) {
-        TRY(d2d(ptrs[t], packed + o2, 2 * kv.first * sizeof(double)));
-        o2 += 2 * kv.first;
-      }
+  TRY(h2d(packed, hp, total * sizeof(double)));
+  TRY(run_batch_dev(c.form(), isign, dp.data(), nn, count, check));
+  TRY(d2h(hp, packed, total * sizeof(double)));
+  CK(cudaStreamSynchronize(g.cur));
+  off = 0;
+  for (size_t t = 0; t < count; ++t) {
+    std::memcpy(ptrs[t], hp + off, 2 * nn[t] * sizeof(double));
+    off += 2 * nn[t];
   }
   return ss.finish(c);
 }
