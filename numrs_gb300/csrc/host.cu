@@ -652,6 +652,7 @@ int run_batch_dev(Form f, int sign, double* const* dptrs, const size_t* nn, size
 }
 
 }  // namespace
+
 }  // namespace gbfft
 
 using namespace gbfft;
@@ -1042,6 +1043,12 @@ int gbfft_power_spectrum(const double* c, size_t nn, double* out, const gbfft_op
   return spectrum_call(1, c, nn, out, opts);
 }
 
+// The sine/cosine transforms turn realft outputs into running sums over n/2
+// terms, which multiplies the FFT's rounding error by up to ~200 at 2^20
+// points.  Double-float arithmetic (about 48 significand bits) would then miss
+// the FP64 bar, so the DF64 form runs their realft in FP64.
+static Form trig_form(Form f) { return f == FORM_DF64 ? FORM_F64 : f; }
+
 static int trig_check(const Call& c, double* y, size_t n, const char* what) {
   TRY(check_form(c));
   if (!y) return fail(GBFFT_INVALID_ARG, "%s: null data", what);
@@ -1076,7 +1083,7 @@ int gbfft_sinft(double* y, size_t n, const gbfft_opts* opts) {
   TRY(trig_work(n, &work, &partial));
   CK(launch_sinft_pre(d, (long long)n, tw, g.cur));
   g.launches++;
-  TRY(realft_dev(c.form(), d, (long long)n, 1));
+  TRY(realft_dev(trig_form(c.form()), d, (long long)n, 1));
   CK(launch_trig_scan(0, d, (long long)n, nullptr, work, g.cur));
   g.launches += 3;
   TRY(unstage(c, y, d, n));
@@ -1097,7 +1104,7 @@ int gbfft_cosft1(double* y, size_t n, const gbfft_opts* opts) {
   TRY(trig_work(n, &work, &partial));
   CK(launch_cosft1_pre(d, (long long)n, partial, tw, g.cur));
   g.launches += 2;
-  TRY(realft_dev(c.form(), d, (long long)n, 1));
+  TRY(realft_dev(trig_form(c.form()), d, (long long)n, 1));
   CK(launch_trig_scan(1, d, (long long)n, partial, work, g.cur));
   g.launches += 3;
   TRY(unstage(c, y, d, n + 1));
@@ -1121,7 +1128,7 @@ int gbfft_cosft2(double* y, size_t n, int isign, const gbfft_opts* opts) {
   if (isign == 1) {
     CK(launch_cosft2_pre(1, d, (long long)n, tw, g.cur));
     g.launches++;
-    TRY(realft_dev(c.form(), d, (long long)n, 1));
+    TRY(realft_dev(trig_form(c.form()), d, (long long)n, 1));
     CK(launch_cosft2_rot(1, d, (long long)n, tw, g.cur));
     g.launches++;
     CK(launch_trig_scan(2, d, (long long)n, nullptr, work, g.cur));
@@ -1131,7 +1138,7 @@ int gbfft_cosft2(double* y, size_t n, int isign, const gbfft_opts* opts) {
     double* w = (double*)g.stage_c.p;
     CK(launch_cosft2_inv_pre(d, w, (long long)n, tw, g.cur));
     g.launches++;
-    TRY(realft_dev(c.form(), w, (long long)n, -1));
+    TRY(realft_dev(trig_form(c.form()), w, (long long)n, -1));
     CK(launch_cosft2_inv_post(w, d, (long long)n, tw, g.cur));
     g.launches++;
   }
