@@ -87,6 +87,19 @@ int gbfft_four1(double* data, size_t nn, int isign, const gbfft_opts* opts);
 int gbfft_four1_batch(double* const* ptrs, const size_t* nn, size_t count, int isign,
                       const gbfft_opts* opts);
 
+/* four1 that allocates nothing.  No counterpart in the crate: it serves
+ * callers that cannot call cudaMalloc when they need a transform (code running
+ * under CUDA graph capture, hosts with a fixed memory budget, plugins inside
+ * another framework's memory pool).  Same transform as gbfft_four1 in FP64,
+ * in place on DEVICE memory `data`, ordered on `stream` (NULL = default).
+ * Its scratch and twiddle tables are fixed arrays in the library image (about
+ * 19 MiB held by every GPU that loads the library, until exit), so nn is
+ * limited to 2^20 (GBFFT_UNSUPPORTED_SIZE above).  The first call on a device
+ * sets it up and waits for that; make it before any stream capture.  Calls
+ * share the scratch array: calls that overlap on the GPU race and must be
+ * ordered by the caller. */
+int gbfft_four1_noalloc(double* data, size_t nn, int isign, void* stream);
+
 /* Uniform batch: `count` transforms of nn points, `dist` doubles apart
  * (dist >= 2*nn). */
 int gbfft_four1_many(double* data, size_t nn, size_t count, size_t dist, int isign,

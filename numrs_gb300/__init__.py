@@ -165,6 +165,23 @@ def four1(data, nn, isign, form="fp64"):
     _check(_lib.load().gbfft_four1(a.ptr, nn, isign, ctypes.byref(o)))
 
 
+def four1_noalloc(data, nn, isign, stream=None):
+    """four1 on a CUDA float64 tensor without any GPU memory allocation.
+
+    For callers that cannot allocate when they transform (graph capture,
+    fixed memory budgets): scratch and tables are fixed arrays inside the
+    library, so nn <= 2^20.  Calls that overlap on the GPU share that scratch;
+    order them.
+    """
+    a = _Arg(data, True)
+    if not a.dev:
+        raise ValueError("four1_noalloc works on device tensors only")
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream().cuda_stream
+    _check(_lib.load().gbfft_four1_noalloc(a.ptr, nn, isign, stream))
+
+
 def four1_optimized(data, nn, isign, form="fp64"):
     """``src/FFT_1.rs:110`` -- same transform as four1 (twiddles are exact on the GPU)."""
     four1(data, nn, isign, form)

@@ -653,6 +653,11 @@ int run_batch_dev(Form f, int sign, double* const* dptrs, const size_t* nn, size
 
 }  // namespace
 
+void record_error(int code, const char* msg) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  fail(code, "%s", msg);
+}
+
 }  // namespace gbfft
 
 using namespace gbfft;
