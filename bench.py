@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="convlv",
-                    choices=["convlv", "four1", "batch", "fourn", "rlft3", "large"])
+                    choices=["convlv", "four1", "batch", "fourn", "rlft3", "large", "c1"])
     ap.add_argument("--form", default="fp64", choices=["fp64", "df64", "fp32"])
     ap.add_argument("--no-forms", action="store_true", help="skip the extra precision forms")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -559,6 +559,156 @@ def run_batch(args, world, rank, local):
     return line
 
 
+def _simple_line(args, world, workload, flops, total_ms, steps, launches, clk, extra=None):
+    hbm, hbm_kind = peaks()
+    line = {
+        "metric": METRIC, "value": flops * steps * world / (total_ms / 1e3) / 1e9,
+        "unit": "GFLOP/s", "n_gpus": world, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.form == "fp64" else args.form,
+        "data": "synthetic", "config": {"workload": workload, "form": args.form},
+        "clocks": clk, "gpu_launches": launches,
+    }
+    if extra:
+        line.update(extra)
+    return line
+
+
+def _timed(args, local, step, flush, steps):
+    import torch
+    import numrs_gb300 as nr
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    nr.launch_count(reset=True)
+    for i in range(steps):
+        if flush is not None:
+            flush.zero_()
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    launches = nr.launch_count()
+    clk = clocks.stop()
+    return sum(a.elapsed_time(b) for a, b in ev), launches, clk
+
+
+def _pass_roofline():
+    import numrs_gb300 as nr
+    hbm, _ = peaks()
+    ms, n, by, fl = nr.profile_read("pass")
+    ach = by / (ms / 1e3) / 1e9 if ms else 0.0
+    return {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+            "traffic": None, "kernel": "k_pass (Stockham pass)", "launches": n,
+            "avg_launch_ms": ms / max(n, 1), "bytes_per_launch": by / max(n, 1),
+            "fp64_tflops_nominal": fl / (ms / 1e3) / 1e12 if ms else 0.0}
+
+
+def _plane_wave_field(shape, dev, seed=0x6B3A2026 + 4, count=32):
+    """uniform[-1,1) plus `count` unit plane waves with integer wave vectors and
+    random phases, generated on the device (same construction as
+    numrs_gb300.workloads.plane_waves)."""
+    import torch
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    x = torch.rand(shape, generator=g, device=dev, dtype=torch.float64) * 2 - 1
+    kv = (torch.rand((count, len(shape)), generator=g, device=dev, dtype=torch.float64) *
+          torch.tensor(shape, device=dev, dtype=torch.float64)).floor()
+    ph = 2 * math.pi * torch.rand(count, generator=g, device=dev, dtype=torch.float64)
+    grids = torch.meshgrid(*[torch.arange(s, device=dev, dtype=torch.float64) / s for s in shape],
+                           indexing="ij")
+    for c in range(count):
+        arg = sum(kv[c, d] * grids[d] for d in range(len(shape)))
+        x += torch.cos(2 * math.pi * arg + ph[c])
+    return x.contiguous()
+
+
+def run_nd(args, world, rank, local):
+    """fourn 256 x 256 x 512 complex, or rlft3 512^3 real; forward + inverse per step."""
+    import torch
+    import numrs_gb300 as nr
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    nr.set_async(True)
+    if args.workload == "fourn":
+        shape = (256, 256, 512)
+        n = int(np.prod(shape))
+        re = _plane_wave_field(shape, dev).reshape(-1)
+        im = _plane_wave_field(shape, dev, seed=0x6B3A2026 + 40).reshape(-1)
+        d = torch.stack([re, im], dim=1).reshape(-1).contiguous()
+        del re, im
+        orig = d.clone()
+
+        def step():
+            nr.fourn(d, shape, 3, 1, form=args.form)
+            nr.fourn(d, shape, 3, -1, form=args.form)
+            d.mul_(1.0 / n)
+        flops = 2 * 5.0 * n * math.log2(n)
+        wl = "fourn 256x256x512 complex f64 (512 MiB), forward + inverse (scaled 1/N) per step"
+    else:
+        shape = (512, 512, 512)
+        n = int(np.prod(shape))
+        d = _plane_wave_field(shape, dev).reshape(-1)
+        orig = d.clone()
+        sp = torch.zeros(512 * 2 * 512, dtype=torch.float64, device=dev)
+
+        def step():
+            nr.rlft3(d, sp, 512, 512, 512, 1, form=args.form)
+            nr.rlft3(d, sp, 512, 512, 512, -1, form=args.form)
+            d.mul_(2.0 / n)
+        flops = 2 * 2.5 * n * math.log2(n)
+        wl = "rlft3 512^3 real f64 (1 GiB) + speq, forward + inverse (scaled 2/N) per step"
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    err = float((d - orig).norm() / orig.norm())
+    steps = min(args.steps, 20)
+    total_ms, launches, clk = _timed(args, local, step, None, steps)
+    nr.profile(True)
+    step()
+    torch.cuda.synchronize()
+    roof = _pass_roofline()
+    nr.profile(False)
+    nr.set_async(False)
+    if rank != 0:
+        return None
+    return _simple_line(args, world, wl, flops, total_ms, steps, launches, clk,
+                        {"roofline": roof, "accuracy": {"roundtrip_rel_l2": err}})
+
+
+def run_c1(args, world, rank, local):
+    """four1 N=4096 round trip (+1, -1, x 1/N): latency of one small transform."""
+    import torch
+    import numrs_gb300 as nr
+    from numrs_gb300 import workloads as W
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    x = W.four1_c1()
+    d = torch.from_numpy(x).to(dev)
+    nr.set_async(True)
+
+    def step():
+        nr.four1(d, 4096, 1, form=args.form)
+        nr.four1(d, 4096, -1, form=args.form)
+        d.mul_(1.0 / 4096)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    steps = max(args.steps, 100)
+    total_ms, launches, clk = _timed(args, local, step, None, steps)
+    nr.set_async(False)
+    err = float(np.linalg.norm(d.cpu().numpy() - x) / np.linalg.norm(x))
+    if rank != 0:
+        return None
+    return _simple_line(args, world, "four1 N=4096 round trip (+1, -1, x1/N), one transform",
+                        2 * 5.0 * 4096 * 12, total_ms, steps, launches, clk,
+                        {"us_per_roundtrip": 1e3 * total_ms / steps,
+                         "accuracy": {"roundtrip_rel_l2": err}})
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -575,8 +725,11 @@ def main():
         line = fn(args, world, rank, local)
         if line:
             print(json.dumps(line), flush=True)
-    elif args.workload != "convlv":
-        raise SystemExit("workload %s is not wired into bench.py yet" % args.workload)
+    elif args.workload in ("fourn", "rlft3", "c1"):
+        fn = run_c1 if args.workload == "c1" else run_nd
+        line = fn(args, world, rank, local)
+        if line:
+            print(json.dumps(line), flush=True)
     else:
         run_convlv(args, world, rank, local)
     if world > 1:

@@ -156,6 +156,14 @@ int gbfft_convlv(const double* data, size_t n, const double* respns, size_t m, i
 int gbfft_correl(const double* data1, size_t n1, const double* data2, size_t n2, double* ans,
                  const gbfft_opts* opts);
 
+/* correl_normalized: src/Correlation.rs:189 (fast = 0: two-pass statistics) and
+ * correl_normalized_fast: :226 (fast = 1: one-pass sums; n <= 32 direct).
+ * Inputs are standardised with their mean and population standard deviation,
+ * then correlated as correl does.  Errors: GBFFT_EMPTY_INPUT,
+ * GBFFT_LENGTH_MISMATCH, GBFFT_ZERO_STD_DEV. */
+int gbfft_correl_normalized(const double* data1, size_t n1, const double* data2, size_t n2,
+                            double* ans, int fast, const gbfft_opts* opts);
+
 /* magnitude_spectrum / power_spectrum: src/FFT_1.rs:206,218.  out[nn]. */
 int gbfft_magnitude_spectrum(const double* c, size_t nn, double* out, const gbfft_opts* opts);
 int gbfft_power_spectrum(const double* c, size_t nn, double* out, const gbfft_opts* opts);

@@ -33,7 +33,9 @@ __all__ = [
     "cosft1", "cosft2", "sinft", "convlv", "correl", "convlv_batch", "correl_batch",
     "autocorrel", "magnitude_spectrum", "power_spectrum", "real_to_complex",
     "complex_to_real", "ConvlvError", "CorrelError", "GbfftError", "launch_count",
-    "FFTBatch", "four1_many", "set_async", "profile", "profile_read",
+    "FFTBatch", "four1_many", "set_async", "profile", "profile_read", "four1_noalloc",
+    "correl_normalized", "correl_normalized_fast", "autocorrel_fast", "ConvlvProcessor",
+    "RealFTProcessor", "TwoFFTProcessor",
 ]
 
 
@@ -369,6 +371,111 @@ def correl(data1, data2, form="fp64", out=None):
         raise CorrelError.LengthMismatch(_lib.last_error())
     _check(st)
     return out[:n]
+
+
+def _correl_norm(data1, data2, fast, form, out):
+    a, b = _Arg(data1, False), _Arg(data2, False)
+    n = a.size
+    if out is None:
+        out = _new_like(a, max(n, 1))
+    o_arg = _Arg(out, True)
+    o = _opts([a, b], form)
+    st = _lib.load().gbfft_correl_normalized(a.ptr, n, b.ptr, b.size, o_arg.ptr, 1 if fast else 0,
+                                             ctypes.byref(o))
+    if st == _lib.EMPTY_INPUT:
+        raise CorrelError.EmptyInput(_lib.last_error())
+    if st == _lib.LENGTH_MISMATCH:
+        raise CorrelError.LengthMismatch(_lib.last_error())
+    if st == _lib.ZERO_STD_DEV:
+        raise CorrelError.ZeroStdDev(_lib.last_error())
+    _check(st)
+    return out[:n]
+
+
+def correl_normalized(data1, data2, form="fp64", out=None):
+    """Pearson-normalised correlation (``src/Correlation.rs:189``)."""
+    return _correl_norm(data1, data2, False, form, out)
+
+
+def correl_normalized_fast(data1, data2, form="fp64", out=None):
+    """One-pass-statistics variant (``src/Correlation.rs:226``)."""
+    return _correl_norm(data1, data2, True, form, out)
+
+
+def autocorrel_fast(data, form="fp64"):
+    """``autocorrel_fast`` (src/Correlation.rs:286): the autocorrelation, as autocorrel."""
+    return correl(data, data, form)
+
+
+class ConvlvProcessor:
+    """Mirror of ``ConvlvProcessor`` (src/Convolve.rs:253-339)."""
+
+    def __init__(self, form="fp64"):
+        self.use_optimized = True
+        self.parallel_threshold = 1024
+        self.form = form
+
+    def with_optimized(self, use_optimized):
+        self.use_optimized = use_optimized
+        return self
+
+    def with_threshold(self, threshold):
+        self.parallel_threshold = threshold
+        return self
+
+    def process(self, data, respns, isign):
+        return convlv(data, respns, isign, self.form)
+
+    def process_batch(self, data_batch, respns, isign):
+        return [self.process(d, respns, isign) for d in data_batch]
+
+
+class RealFTProcessor:
+    """Mirror of ``RealFTProcessor`` (src/Real_FT.rs:332-370)."""
+
+    def __init__(self, form="fp64"):
+        self.use_optimized = True
+        self.parallel_threshold = 1024
+        self.form = form
+
+    def with_optimized(self, use_optimized):
+        self.use_optimized = use_optimized
+        return self
+
+    def with_threshold(self, threshold):
+        self.parallel_threshold = threshold
+        return self
+
+    def process(self, data, n, isign):
+        realft(data, n, isign, self.form)
+
+    def process_batch(self, batches):
+        for data, n, isign in batches:
+            self.process(data, n, isign)
+
+
+class TwoFFTProcessor:
+    """Mirror of ``TwoFFTProcessor`` (src/FFT_2.rs:222-265)."""
+
+    def __init__(self, form="fp64"):
+        self.use_optimized = True
+        self.parallel_threshold = 1024
+        self.form = form
+
+    def with_optimized(self, use_optimized):
+        self.use_optimized = use_optimized
+        return self
+
+    def with_threshold(self, threshold):
+        self.parallel_threshold = threshold
+        return self
+
+    def process(self, data1, data2, fft1, fft2):
+        twofft(data1, data2, fft1, fft2, self.form)
+
+    def process_batch(self, batches):
+        for data1, data2, fft1, fft2 in batches:
+            self.process(data1, data2, fft1, fft2)
 
 
 def convlv_batch(data_batch, respns, isign, form="fp64"):

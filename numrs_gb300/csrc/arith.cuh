@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
+#include "conv.cuh"
+
 namespace gbfft {
 
 struct alignas(16) d2 { double x, y; };
@@ -103,12 +105,13 @@ struct F32 {
   __device__ __forceinline__ static C conj(C a) { return {a.x, -a.y}; }
   __device__ __forceinline__ static S to_s(C a) { return {a.x, a.y}; }
   __device__ __forceinline__ static C from_s(S s) { return {s.x, s.y}; }
+  // conversions on the integer/FP32 pipes (conv.cuh), not GB300's FP64 pipe
   __device__ __forceinline__ static C from_d(double a, double b) {
-    return {__double2float_rn(a), __double2float_rn(b)};
+    return {conv::d2f(a), conv::d2f(b)};
   }
   __device__ __forceinline__ static void to_d(C a, double& x, double& y) {
-    x = (double)a.x;
-    y = (double)a.y;
+    x = conv::f2d(a.x);
+    y = conv::f2d(a.y);
   }
   __device__ __forceinline__ static C ld_tw(const TW* p, int sg) {
     f2 t = *p;
@@ -177,12 +180,13 @@ __device__ __forceinline__ df df_scale_f(df a, float s) {  // s exact float cons
   e = __fmaf_rn(a.lo, s, e);
   return fast_two_sum(p, e);
 }
+// conversions on the integer/FP32 pipes (conv.cuh), not GB300's FP64 pipe
 __device__ __forceinline__ df df_from_double(double v) {
-  float h = __double2float_rn(v);
-  float l = __double2float_rn(v - (double)h);
-  return {h, l};
+  df r;
+  conv::d2df(v, r.hi, r.lo);
+  return r;
 }
-__device__ __forceinline__ double df_to_double(df a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ double df_to_double(df a) { return conv::df2d(a.hi, a.lo); }
 
 struct DF64 {
   static constexpr int kind = 2;

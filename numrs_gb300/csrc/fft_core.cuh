@@ -217,23 +217,6 @@ template <> struct IOElem<IO_D2> { using T = d2; };
 template <> struct IOElem<IO_F2> { using T = f2; };
 template <> struct IOElem<IO_F4> { using T = f4; };
 
-template <class F, int IO, bool L2_ONLY>
-__device__ __forceinline__ typename F::C gload_elem(const void* base, long long i) {
-  using E = typename IOElem<IO>::T;
-  const E* p = reinterpret_cast<const E*>(base) + i;
-  if constexpr (L2_ONLY) {
-    if constexpr (IO == IO_F2) {
-      float2 v = __ldcg(reinterpret_cast<const float2*>(p));
-      return gload<F, IO>(&v, 0);
-    } else {
-      float4 v = __ldcg(reinterpret_cast<const float4*>(p));
-      return gload<F, IO>(&v, 0);
-    }
-  } else {
-    return gload<F, IO>(p, 0);
-  }
-}
-
 template <class F, int SG, int IN, int OUT, int T, bool L2_ONLY>
 __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
                                           typename F::S* sm, int tid) {
@@ -260,7 +243,10 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
   const long long lqmask = (1ll << p.lq_log) - 1;
 
   // ---- load tile: global -> (twiddle) -> shared ----
-#pragma unroll 4
+  // All sixteen loads of a thread are issued before any is used, so that each
+  // SM keeps enough bytes in flight to cover the memory latency.
+  IE raw[kEPT];
+#pragma unroll
   for (int k = 0; k < kEPT; ++k) {
     const int e = tid + k * T;
     int c, r;
@@ -268,18 +254,37 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
     else { c = e & (Cn - 1); r = e >> logC; }
     long long line = line0, j = j0;
     if (p.mode == 0) j += c; else line += c;
-    C v;
     if (line < p.nlines) {
       const IE* base = p.in_ptrs
           ? reinterpret_cast<const IE*>(p.in_ptrs[line])
           : reinterpret_cast<const IE*>(p.in) + ((line >> p.lq_log) * p.lstride + (line & lqmask));
-      v = gload_elem<F, IN, L2_ONLY>(base, (j + ((long long)r << logLR)) * p.s);
-      if (p.logNs > 0) {
-        const long long jm = j & (p.Ns - 1);
-        if (jm != 0 && r != 0) v = F::mul(v, twiddle<F>(p.tw, p.logNs + logR, jm * r, SG));
+      const IE* src = base + (j + ((long long)r << logLR)) * p.s;
+      if constexpr (L2_ONLY) {
+        if constexpr (sizeof(IE) == 8) {
+          float2 t = __ldcg(reinterpret_cast<const float2*>(src));
+          memcpy(&raw[k], &t, 8);
+        } else {
+          float4 t = __ldcg(reinterpret_cast<const float4*>(src));
+          memcpy(&raw[k], &t, 16);
+        }
+      } else {
+        raw[k] = *src;
       }
     } else {
-      v = F::from_d(0.0, 0.0);
+      memset(&raw[k], 0, sizeof(IE));
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kEPT; ++k) {
+    const int e = tid + k * T;
+    int c, r;
+    if (p.in_rcontig) { r = e & (R - 1); c = e >> logR; }
+    else { c = e & (Cn - 1); r = e >> logC; }
+    C v = gload<F, IN>(&raw[k], 0);
+    if (p.logNs > 0) {
+      const long long j = (p.mode == 0) ? j0 + c : j0;
+      const long long jm = j & (p.Ns - 1);
+      if (jm != 0 && r != 0) v = F::mul(v, twiddle<F>(p.tw, p.logNs + logR, jm * r, SG));
     }
     sm[pidx((c << logR) + r, sh)] = F::to_s(v);
   }

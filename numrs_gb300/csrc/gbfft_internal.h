@@ -127,6 +127,14 @@ cudaError_t launch_cosft2_inv_post(const double* w, double* y, long long n, Twid
 cudaError_t launch_trig_scan(int kind, double* y, long long n, double* partial, double* work,
                              cudaStream_t st);
 cudaError_t launch_scale(double* data, long long count, double s, cudaStream_t st);
+// Normalised correlation helpers (src/Correlation.rs:189-270).
+cudaError_t launch_correl_direct_centered(const double* a, const double* b, double* out,
+                                          long long n, double ma, double mb, double norm,
+                                          cudaStream_t st);
+cudaError_t launch_moment(const double* x, long long n, double shift, int p, double* partial,
+                          double* out, cudaStream_t st);
+cudaError_t launch_standardize(const double* x, long long n, double mean, double stdv,
+                               double* out, cudaStream_t st);
 cudaError_t launch_spectrum(int kind, const double* c, double* out, long long nn,
                             cudaStream_t st);
 

@@ -2,6 +2,7 @@
 // axis plans (Stockham pass schedules), scratch management and the entry
 // points declared in include/gbfft.h.
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -199,12 +200,24 @@ void split_subpasses(int logR, PassParams& p) {
   for (int i = 0; i < nsub; ++i) p.q[i] = base + (i < extra ? 1 : 0);
 }
 
+// Latency mode: one or two small transforms (at most 8192 points in all) would
+// run on one or two SMs in a single pass, and an FP64 transform of 4096 points
+// then takes ~40 us on one SM.  Two passes of 512-point tiles spread the same
+// work over 8-16 SMs.
+constexpr long long kLatencyMaxWork = 8192;
+constexpr int kLatencyTileLog = 9;
+
 AxisPlan make_axis_plan(long long L, long long s, long long nlines, int lq_log,
                         long long lstride, bool full_tile = false) {
   AxisPlan ap;
   const int logL = ilog2((unsigned long long)L);
   std::vector<int> radix;
-  if (logL <= 12) {
+  const bool latency = !full_tile && s == 1 && logL >= 10 && logL <= 12 &&
+                       L * nlines <= kLatencyMaxWork;
+  if (latency) {
+    radix.push_back((logL + 1) / 2);
+    radix.push_back(logL / 2);
+  } else if (logL <= 12) {
     radix.push_back(logL);
   } else {
     int P = (logL + kMaxPassLog - 1) / kMaxPassLog;
@@ -233,7 +246,8 @@ AxisPlan make_axis_plan(long long L, long long s, long long nlines, int lq_log,
     int logC;
     if (s == 1 && LR > 1) {
       p.mode = 0;
-      logC = std::min(ilog2(kTileE) - logR, ilog2((unsigned long long)LR));
+      const int tileLog = latency ? kLatencyTileLog : ilog2(kTileE);
+      logC = std::min(tileLog - logR, ilog2((unsigned long long)LR));
       p.in_rcontig = 0;
       p.out_rcontig = (logNs == 0) ? 1 : 0;
     } else {
@@ -1016,6 +1030,92 @@ int gbfft_correl(const double* data1, size_t n1, const double* data2, size_t n2,
   if (!is_pow2(n) || ilog2(n) > kMaxAxisLog)
     return fail(GBFFT_UNSUPPORTED_SIZE, "correl: n=%zu must be a power of two when > 32", n);
   return spectral_call(c, 2, data1, data2, n, n, ans);
+}
+
+// correl_normalized (fast = 0, src/Correlation.rs:189-223) and
+// correl_normalized_fast (fast = 1, :226-270).  The statistics are computed on
+// the GPU; the host reads the four scalars back to decide ZeroStdDev.
+int gbfft_correl_normalized(const double* data1, size_t n1, const double* data2, size_t n2,
+                            double* ans, int fast, const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  if (n1 == 0) return fail(GBFFT_EMPTY_INPUT, "correl_normalized: input arrays cannot be empty");
+  if (n2 != n1) return fail(GBFFT_LENGTH_MISMATCH, "correl_normalized: input arrays must have the same length");
+  if (!data1 || !data2 || !ans) return fail(GBFFT_INVALID_ARG, "correl_normalized: null pointer");
+  const size_t n = n1;
+  if (n > 32 && (!is_pow2(n) || ilog2(n) > kMaxAxisLog))
+    return fail(GBFFT_UNSUPPORTED_SIZE, "correl_normalized: n=%zu must be a power of two when > 32", n);
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  // device copies: inputs (staged for host pointers) and z-scores
+  const size_t need = 4 * n + 256 + 8;
+  TRY(ensure(g.stage_c, need * sizeof(double)));
+  double* base = (double*)g.stage_c.p;
+  const double *a = data1, *b = data2;
+  if (!c.dev()) {
+    TRY(h2d(base, data1, n * sizeof(double)));
+    TRY(h2d(base + n, data2, n * sizeof(double)));
+    a = base;
+    b = base + n;
+  }
+  double* za = base + 2 * n;
+  double* zb = base + 3 * n;
+  double* partial = base + 4 * n;
+  double* scal = partial + 256;  // sum1, sum2, m2_1, m2_2
+  const double nd = (double)n;
+  double h[4] = {0, 0, 0, 0};
+  CK(launch_moment(a, (long long)n, 0.0, 1, partial, scal, g.cur));
+  CK(launch_moment(b, (long long)n, 0.0, 1, partial, scal + 1, g.cur));
+  if (fast) {
+    CK(launch_moment(a, (long long)n, 0.0, 2, partial, scal + 2, g.cur));
+    CK(launch_moment(b, (long long)n, 0.0, 2, partial, scal + 3, g.cur));
+    g.launches += 8;
+    TRY(d2h(h, scal, 4 * sizeof(double)));
+    CK(cudaStreamSynchronize(g.cur));
+  } else {
+    g.launches += 4;
+    TRY(d2h(h, scal, 2 * sizeof(double)));
+    CK(cudaStreamSynchronize(g.cur));
+    CK(launch_moment(a, (long long)n, h[0] / nd, 2, partial, scal + 2, g.cur));
+    CK(launch_moment(b, (long long)n, h[1] / nd, 2, partial, scal + 3, g.cur));
+    g.launches += 4;
+    TRY(d2h(h + 2, scal + 2, 2 * sizeof(double)));
+    CK(cudaStreamSynchronize(g.cur));
+  }
+  const double m1 = h[0] / nd, m2 = h[1] / nd;
+  const double s1 = fast ? std::sqrt(h[2] / nd - m1 * m1) : std::sqrt(h[2] / nd);
+  const double s2 = fast ? std::sqrt(h[3] / nd - m2 * m2) : std::sqrt(h[3] / nd);
+  if (s1 == 0.0 || s2 == 0.0 || std::isnan(s1) || std::isnan(s2))
+    return fail(GBFFT_ZERO_STD_DEV, "Normalization error: standard deviation is zero");
+  double* out = ans;
+  if (!c.dev()) out = za;  // result staged in the z buffer after use below
+  if (fast && n <= 32) {
+    double* o = c.dev() ? ans : zb;
+    CK(launch_correl_direct_centered(a, b, o, (long long)n, m1, m2, 1.0 / (s1 * s2 * nd), g.cur));
+    g.launches++;
+    if (!c.dev()) TRY(d2h(ans, zb, n * sizeof(double)));
+    return ss.finish(c);
+  }
+  CK(launch_standardize(a, (long long)n, m1, s1, za, g.cur));
+  CK(launch_standardize(b, (long long)n, m2, s2, zb, g.cur));
+  g.launches += 2;
+  if (n <= 32) {
+    double* o = c.dev() ? ans : partial;
+    CK(launch_correl_direct(za, zb, o, (long long)n, g.cur));
+    g.launches++;
+    if (!c.dev()) TRY(d2h(ans, o, n * sizeof(double)));
+    return ss.finish(c);
+  }
+  TRY(ensure(g.work, 2 * n * sizeof(double)));
+  double* w = (double*)g.work.p;
+  TRY(d2d(w, za, n * sizeof(double)));
+  TRY(d2d(w + n, zb, n * sizeof(double)));
+  TRY(spectral_dev(c.form(), 2, w, (long long)n));
+  (void)out;
+  if (c.dev()) TRY(d2d(ans, w, n * sizeof(double)));
+  else TRY(d2h(ans, w, n * sizeof(double)));
+  return ss.finish(c);
 }
 
 static int spectrum_call(int kind, const double* cdata, size_t nn, double* out,

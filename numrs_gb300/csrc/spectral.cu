@@ -83,6 +83,20 @@ __device__ __forceinline__ void twist_pair(typename F::C& zk, typename F::C& zm,
   zm = F::conj(F::sub(h1, t));
 }
 
+// The same twist without its two factors of 1/2: returns 2 Z_k and 2 Z_m.
+// The fused spectral kernel folds those factors into its one product scale.
+template <class F, int IS>
+__device__ __forceinline__ void twist2_pair(typename F::C& zk, typename F::C& zm,
+                                            typename F::C w) {
+  using C = typename F::C;
+  C czm = F::conj(zm);
+  C h1 = F::add(zk, czm);
+  C h2 = F::mul_j(F::sub(zk, czm), -IS);
+  C t = F::mul(h2, w);
+  zk = F::add(h1, t);
+  zm = F::conj(F::sub(h1, t));
+}
+
 template <class F>
 __device__ __forceinline__ typename F::C ldc(const double* p, long long k) {
   d2 v = reinterpret_cast<const d2*>(p)[k];
@@ -151,8 +165,11 @@ cudaError_t launch_realft_twist(Form f, int isign, double* data, long long n, lo
 // both, product scaled by 1/(n/2), inverse twist -- the packed input of the
 // inverse n/2-point FFT, written to out (which may alias a).
 // ---------------------------------------------------------------------------
+// x, y are `pre` times the true spectra (pre = 1 or 2; exact powers of two
+// keep every comparison and quotient identical).
 template <class F, int KIND>
-__device__ __forceinline__ typename F::C spec_prod(typename F::C x, typename F::C y, double inv_no2) {
+__device__ __forceinline__ typename F::C spec_prod(typename F::C x, typename F::C y, double inv_no2,
+                                                   double pre = 1.0) {
   using C = typename F::C;
   if constexpr (KIND == 0) {
     return F::scale(F::mul(x, y), inv_no2);
@@ -165,7 +182,7 @@ __device__ __forceinline__ typename F::C spec_prod(typename F::C x, typename F::
     F::to_d(y, yr, yi);
     double mag2 = yr * yr + yi * yi;
     double o_r = 0.0, o_i = 0.0;
-    if (!(mag2 < 1e-12)) {
+    if (!(mag2 < 1e-12 * pre * pre)) {
       o_r = (xr * yr + xi * yi) / mag2 * inv_no2;
       o_i = (xi * yr - xr * yi) / mag2 * inv_no2;
     }
@@ -216,11 +233,13 @@ __global__ void k_spectral(const double* a, const double* b, double* out, long l
     const long long m = n / 2 - k;
     C ak = ldc<F>(a, k), am = ldc<F>(a, m), bk = ldc<F>(b, k), bm = ldc<F>(b, m);
     C w = twiddle<F>(tw, logn, k, 1);
-    twist_pair<F, 1>(ak, am, w);
-    twist_pair<F, 1>(bk, bm, w);
-    C pk = spec_prod<F, KIND>(ak, bk, inv_no2);
-    C pm = spec_prod<F, KIND>(am, bm, inv_no2);
-    twist_pair<F, -1>(pk, pm, F::conj(w));
+    // unscaled twists give 2A and 2B; the unscaled inverse twist doubles again
+    twist2_pair<F, 1>(ak, am, w);
+    twist2_pair<F, 1>(bk, bm, w);
+    const double sc = (KIND == 1) ? 0.5 * inv_no2 : 0.125 * inv_no2;
+    C pk = spec_prod<F, KIND>(ak, bk, sc, 2.0);
+    C pm = spec_prod<F, KIND>(am, bm, sc, 2.0);
+    twist2_pair<F, -1>(pk, pm, F::conj(w));
     stc<F>(out, k, pk);
     stc<F>(out, m, pm);
   }
@@ -283,6 +302,79 @@ __global__ void k_correl_direct(const double* a, const double* b, double* out, l
 cudaError_t launch_correl_direct(const double* a, const double* b, double* out, long long n,
                                  cudaStream_t st) {
   k_correl_direct<<<1, 32, 0, st>>>(a, b, out, n);
+  return cudaGetLastError();
+}
+
+// Centered direct linear correlation for correl_normalized_fast's n <= 32
+// branch (src/Correlation.rs:251-263): out[lag] = norm * sum (a-ma)(b-mb).
+__global__ void k_correl_direct_centered(const double* a, const double* b, double* out,
+                                         long long n, double ma, double mb, double norm) {
+  long long lag = threadIdx.x;
+  if (lag >= n) return;
+  double sum = 0.0;
+  for (long long i = 0; i < n - lag; ++i) sum += (a[i + lag] - ma) * (b[i] - mb);
+  out[lag] = sum * norm;
+}
+
+cudaError_t launch_correl_direct_centered(const double* a, const double* b, double* out,
+                                          long long n, double ma, double mb, double norm,
+                                          cudaStream_t st) {
+  k_correl_direct_centered<<<1, 32, 0, st>>>(a, b, out, n, ma, mb, norm);
+  return cudaGetLastError();
+}
+
+// Per-block partial sums of (x - shift)^p, p = 1 or 2, for the normalised
+// correlation's statistics; 256 blocks, summed in a fixed order afterwards.
+__global__ void k_block_moment(const double* x, long long n, double shift, int p,
+                               double* partial) {
+  __shared__ double red[256];
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double d = x[i] - shift;
+    acc += (p == 2) ? d * d : d;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s2 = blockDim.x / 2; s2 > 0; s2 >>= 1) {
+    if ((int)threadIdx.x < s2) red[threadIdx.x] += red[threadIdx.x + s2];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void k_sum256(const double* partial, double* out) {
+  __shared__ double red[256];
+  red[threadIdx.x] = partial[threadIdx.x];
+  __syncthreads();
+  for (int s2 = 128; s2 > 0; s2 >>= 1) {
+    if ((int)threadIdx.x < s2) red[threadIdx.x] += red[threadIdx.x + s2];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+// out = sum over the array of (x - shift)^p; partial holds 256 doubles.
+cudaError_t launch_moment(const double* x, long long n, double shift, int p, double* partial,
+                          double* out, cudaStream_t st) {
+  k_block_moment<<<256, 256, 0, st>>>(x, n, shift, p, partial);
+  k_sum256<<<1, 256, 0, st>>>(partial, out);
+  return cudaGetLastError();
+}
+
+__global__ void k_standardize(const double* x, long long n, double mean, double stdv,
+                              double* out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = (x[i] - mean) / stdv;
+}
+
+cudaError_t launch_standardize(const double* x, long long n, double mean, double stdv,
+                               double* out, cudaStream_t st) {
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  k_standardize<<<blocks, 256, 0, st>>>(x, n, mean, stdv, out);
   return cudaGetLastError();
 }
 

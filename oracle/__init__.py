@@ -45,6 +45,8 @@ def lib():
         L.orc_convlv.restype = ctypes.c_int
         L.orc_correl.argtypes = [_dp, _sz, _dp, _sz, _dp]
         L.orc_correl.restype = ctypes.c_int
+        L.orc_correl_normalized.argtypes = [_dp, _sz, _dp, _sz, _dp, ctypes.c_int]
+        L.orc_correl_normalized.restype = ctypes.c_int
         L.orc_magnitude_spectrum.argtypes = [_dp, _sz, _dp]
         L.orc_power_spectrum.argtypes = [_dp, _sz, _dp]
         L.orc_dft_ld.argtypes = [_dp, _sz, ctypes.c_int, _dp]
@@ -141,6 +143,18 @@ def correl(data1, data2):
     ans = np.zeros(max(n, 1))
     st = lib().orc_correl(_ptr(data1) if n else None, n, _ptr(data2) if data2.size else None,
                           data2.size, _ptr(ans))
+    return st, ans[:n]
+
+
+def correl_normalized(data1, data2, fast=False):
+    """Returns (status, ans); status 5 = ZeroStdDev."""
+    data1 = np.ascontiguousarray(data1, dtype=np.float64)
+    data2 = np.ascontiguousarray(data2, dtype=np.float64)
+    n = data1.size
+    ans = np.zeros(max(n, 1))
+    st = lib().orc_correl_normalized(_ptr(data1) if n else None, n,
+                                     _ptr(data2) if data2.size else None, data2.size, _ptr(ans),
+                                     1 if fast else 0)
     return st, ans[:n]
 
 

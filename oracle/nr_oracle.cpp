@@ -728,6 +728,56 @@ int orc_correl(const double* data1, size_t n1, const double* data2, size_t n2, d
   return 0;
 }
 
+// correl_normalized (fast = 0, src/Correlation.rs:189-223) and
+// correl_normalized_fast (fast = 1, :226-270).  Return codes as orc_correl,
+// plus 5 for ZeroStdDev.
+int orc_correl_normalized(const double* d1, size_t n1, const double* d2, size_t n2, double* ans,
+                          int fast) {
+  if (n1 == 0) return 1;
+  if (n2 != n1) return 2;
+  const size_t n = n1;
+  const double nd = (double)n;
+  double mean1, mean2, std1, std2;
+  if (!fast) {
+    double s1 = 0, s2 = 0;
+    for (size_t i = 0; i < n; ++i) { s1 += d1[i]; s2 += d2[i]; }
+    mean1 = s1 / nd;
+    mean2 = s2 / nd;
+    double v1 = 0, v2 = 0;
+    for (size_t i = 0; i < n; ++i) {
+      v1 += (d1[i] - mean1) * (d1[i] - mean1);
+      v2 += (d2[i] - mean2) * (d2[i] - mean2);
+    }
+    std1 = std::sqrt(v1 / nd);
+    std2 = std::sqrt(v2 / nd);
+  } else {
+    double s1 = 0, s2 = 0, q1 = 0, q2 = 0;
+    for (size_t i = 0; i < n; ++i) {
+      s1 += d1[i]; s2 += d2[i]; q1 += d1[i] * d1[i]; q2 += d2[i] * d2[i];
+    }
+    mean1 = s1 / nd;
+    mean2 = s2 / nd;
+    std1 = std::sqrt(q1 / nd - mean1 * mean1);
+    std2 = std::sqrt(q2 / nd - mean2 * mean2);
+  }
+  if (std1 == 0.0 || std2 == 0.0 || std::isnan(std1) || std::isnan(std2)) return 5;
+  if (fast && n <= 32) {
+    const double norm = 1.0 / (std1 * std2 * nd);
+    for (size_t lag = 0; lag < n; ++lag) {
+      double sum = 0.0;
+      for (size_t i = 0; i < n - lag; ++i) sum += (d1[i + lag] - mean1) * (d2[i] - mean2);
+      ans[lag] = sum * norm;
+    }
+    return 0;
+  }
+  std::vector<double> z1(n), z2(n);
+  for (size_t i = 0; i < n; ++i) {
+    z1[i] = (d1[i] - mean1) / std1;
+    z2[i] = (d2[i] - mean2) / std2;
+  }
+  return orc_correl(z1.data(), n, z2.data(), n, ans);
+}
+
 // magnitude_spectrum / power_spectrum (src/FFT_1.rs:206-228).
 void orc_magnitude_spectrum(const double* c, size_t nn, double* out) {
   for (size_t k = 0; k < nn; ++k) out[k] = std::sqrt(c[2 * k] * c[2 * k] + c[2 * k + 1] * c[2 * k + 1]);

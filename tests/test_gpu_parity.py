@@ -281,6 +281,37 @@ def test_correl_kats(nr):
     assert abs(res[0][0] - 5.0) < 1e-10 and abs(res[1][0] - 25.0) < 1e-10
 
 
+@pytest.mark.parametrize("fast", [False, True])
+@pytest.mark.parametrize("n", [4, 16, 32, 64, 4096])
+def test_correl_normalized(nr, fast, n):
+    a, b = W.normal(n + 30, n), W.normal(n + 31, n) + 0.5
+    fn = nr.correl_normalized_fast if fast else nr.correl_normalized
+    got = fn(a, b)
+    st, ref = O.correl_normalized(a, b, fast=fast)
+    assert st == 0
+    assert_fp64_close(got, ref, max(1, n.bit_length() - 1), "correl_normalized n=%d" % n)
+    assert abs(nr.correl_normalized_fast([1.0, 2.0, 3.0, 4.0], [1.0, 2.0, 3.0, 4.0])[0] - 1.0) < 1e-10
+    with pytest.raises(nr.CorrelError.ZeroStdDev):
+        nr.correl_normalized([2.0, 2.0, 2.0], [1.0, 2.0, 3.0])
+
+
+def test_processors(nr):
+    x = W.normal(3, 1024)
+    d = x.copy()
+    nr.RealFTProcessor().process(d, 1024, 1)
+    ref = x.copy()
+    O.realft(ref, 1024, 1)
+    assert_fp64_close(d, ref, 10, "RealFTProcessor")
+    r = W.normal(4, 33)
+    got = nr.ConvlvProcessor().process_batch([x, x[::-1].copy()], r, 1)
+    for g_, xx in zip(got, [x, x[::-1].copy()]):
+        assert_fp64_close(g_, O.convlv(xx, r, 1)[1], 10, "ConvlvProcessor")
+    f1, f2 = np.zeros(2050), np.zeros(2050)
+    nr.TwoFFTProcessor().process(x, x * 2, f1, f2)
+    r1, r2 = O.twofft(x, x * 2)
+    assert_fp64_close(f1[:2048], r1[:2048], 10, "TwoFFTProcessor")
+
+
 def test_correl_golden(nr):
     g = np.load(GOLD)
     got = nr.correl(g["convlv_1024_data"], g["correl_1024_b"])

@@ -211,6 +211,23 @@ def test_correl_kats_and_circular():
         assert st == 0 and rel_l2(c, ref) < 1e-13
 
 
+def test_correl_normalized_kats():
+    # src/Correlation.rs:505-512: the fast form is 1 at lag 0 for identical inputs
+    st, r = O.correl_normalized([1, 2, 3, 4], [1, 2, 3, 4], fast=True)
+    assert st == 0 and abs(r[0] - 1.0) < 1e-10
+    # the two-pass form standardises and correlates directly for n <= 32: lag 0
+    # is n (the reference's test at :435-450 expects 1, which holds for neither form)
+    st, r = O.correl_normalized([1, 2, 3, 4], [1, 2, 3, 4])
+    assert st == 0 and abs(r[0] - 4.0) < 1e-10
+    assert O.correl_normalized([2, 2, 2], [1, 2, 3])[0] == 5  # ZeroStdDev
+    a, b = W.normal(1, 256), W.normal(2, 256)
+    st, r = O.correl_normalized(a, b)
+    za = (a - a.mean()) / a.std()
+    zb = (b - b.mean()) / b.std()
+    ref = np.array([np.dot(np.roll(za, -k), zb) for k in range(256)])
+    assert st == 0 and rel_l2(r, ref) < 1e-13
+
+
 def test_golden_fixtures_reproduce():
     g = np.load(GOLD)
     d = g["four1_4096_in"].copy()
