@@ -52,6 +52,7 @@ struct Ctx {
   std::vector<char> host_pack;
   std::string err;
   long long launches = 0;
+  bool host_direct = false;  // kernels may read/write the caller's host arrays
   bool profiling = false;
   std::vector<ProfRec> prof;
   std::vector<cudaEvent_t> evpool;
@@ -120,6 +121,14 @@ int init_locked(int device) {
   CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
   g.cur = g.stream;
   g.device = device;
+  // On systems where the GPU reaches pageable host memory through the host's
+  // page tables (Grace + GB300 over NVLink-C2C), host-pointer calls let the
+  // first pass read the caller's arrays and the last pass write them, so the
+  // link transfers overlap the compute instead of preceding and following it.
+  int pma = 0;
+  cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+  const char* env = getenv("GBFFT_HOST_DIRECT");
+  g.host_direct = pma != 0 && !(env && env[0] == '0');
   g.inited = true;
   return GBFFT_OK;
 }
@@ -318,6 +327,29 @@ int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale = 1.
       p.scale = scale;
     }
     TRY(launch_pass(f, sign, ps.in_user ? IO_D2 : sio, ps.out_user ? IO_D2 : sio, p, ps.threads));
+  }
+  return GBFFT_OK;
+}
+
+// Out-of-place run of a one- or two-pass plan: the first pass reads `in` (or
+// the per-line pointers `in_lines`, a device array), the last pass writes
+// `out`.  Either may be host memory when g.host_direct is set.
+int run_axis_io(Form f, int sign, const AxisPlan& ap, const void* in,
+                const void* const* in_lines, void* out) {
+  Twiddles tw;
+  TRY(tables(f, tw));
+  const IOType sio = scratch_io(f);
+  const size_t P = ap.passes.size();
+  if (P > 2) return fail(GBFFT_INVALID_ARG, "run_axis_io: %zu passes", P);
+  if (P == 2) TRY(ensure(g.scratch, ap.scratch_elems * io_bytes(sio)));
+  for (size_t i = 0; i < P; ++i) {
+    PassParams p = ap.passes[i].p;
+    p.tw = tw;
+    const bool first = i == 0, last = i + 1 == P;
+    p.in = first ? in : g.scratch.p;
+    p.in_ptrs = first ? in_lines : nullptr;
+    p.out = last ? out : g.scratch.p;
+    TRY(launch_pass(f, sign, first ? IO_D2 : sio, last ? IO_D2 : sio, p, ap.passes[i].threads));
   }
   return GBFFT_OK;
 }
@@ -665,6 +697,41 @@ int run_batch_dev(Form f, int sign, double* const* dptrs, const size_t* nn, size
   return GBFFT_OK;
 }
 
+// convlv / correl with the caller's host arrays read and written by the
+// kernels themselves (g.host_direct; n >= 4): the first forward pass reads data
+// (and, for correl, data2) from the host, the last inverse pass writes ans.
+int spectral_direct(Form f, int kind, const double* a, const double* b, long long n, long long m,
+                    double* ans) {
+  Twiddles tw;
+  TRY(tables(f, tw));
+  const long long nh = n / 2;
+  TRY(ensure(g.work, 2 * (size_t)n * sizeof(double)));
+  double* w = (double*)g.work.p;
+  const void* lines[2];
+  lines[0] = a;
+  if (kind == 2) {
+    lines[1] = b;
+  } else {
+    CK(launch_expand_response(b, m, w + n, n, nullptr, nullptr, g.cur));
+    g.launches++;
+    lines[1] = w + n;
+  }
+  TRY(ensure(g.ptrtab, 64));
+  CK(cudaMemcpyAsync(g.ptrtab.p, lines, sizeof lines, cudaMemcpyHostToDevice, g.cur));
+  TRY(run_axis_io(f, 1, axis_plan(nh, 1, 2, 0, nh), nullptr, (const void* const*)g.ptrtab.p, w));
+  {
+    ProfScope ps(PK_SPECTRAL, 3.0 * n * 8);
+    CK(launch_spectral_product(f, kind, w, w + n, w, n, tw, g.cur));
+  }
+  g.launches++;
+  TRY(run_axis_io(f, -1, axis_plan(nh, 1, 1, 0, nh), w, nullptr, ans));
+  return GBFFT_OK;
+}
+
+// Whether a plan of this length can run with host arrays read and written by
+// its first and last passes.
+bool direct_fits(long long L) { return g.host_direct && L <= (1ll << kBatchMaxLog); }
+
 }  // namespace
 
 void record_error(int code, const char* msg) {
@@ -761,6 +828,12 @@ int gbfft_four1(double* data, size_t nn, int isign, const gbfft_opts* opts) {
     return fail(GBFFT_UNSUPPORTED_SIZE, "four1: nn=%zu must be a power of two <= 2^%d", nn, kMaxAxisLog);
   TRY(init_locked(g.device));
   StreamScope ss(c);
+  if (!c.dev() && nn > 1 && direct_fits((long long)nn)) {
+    // the first pass reads the caller's array, the last pass writes it back
+    TRY(run_axis_io(c.form(), isign, axis_plan((long long)nn, 1, 1, 0, (long long)nn), data,
+                    nullptr, data));
+    return ss.finish(c);
+  }
   double* d;
   TRY(stage_inout(c, g.stage_a, data, 2 * nn, &d));
   TRY(fft_lines(c.form(), isign, d, (long long)nn, 1, (long long)nn));
@@ -959,6 +1032,10 @@ static int spectral_call(const Call& c, int kind, const double* a, const double*
                          size_t m, double* ans) {
   TRY(init_locked(g.device));
   StreamScope ss(c);
+  if (!c.dev() && n >= 4 && direct_fits((long long)n / 2)) {
+    TRY(spectral_direct(c.form(), kind, a, b, (long long)n, (long long)m, ans));
+    return ss.finish(c);
+  }
   TRY(ensure(g.work, 2 * n * sizeof(double)));
   double* w = (double*)g.work.p;
   const double *da = a, *db = b;

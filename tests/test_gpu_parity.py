@@ -398,6 +398,26 @@ def test_large_roundtrip_properties(nr):
     assert rel_l2(d, x) < 1e-13
 
 
+def test_host_and_device_paths_agree(nr):
+    """Host arrays (read and written by the kernels directly where the device
+    supports it, staged otherwise) and device tensors give the same results."""
+    torch = pytest.importorskip("torch")
+    for n in (64, 4096, 1 << 16, 1 << 20):
+        x, r = W.normal(n + 50, n), W.normal(n + 51, n)
+        h = nr.convlv(x, r, 1)
+        d = nr.convlv(torch.from_numpy(x).cuda(), torch.from_numpy(r).cuda(), 1).cpu().numpy()
+        assert_fp64_close(h, d, n.bit_length() - 1, "convlv host vs device n=%d" % n)
+        hc = nr.correl(x, r)
+        dc = nr.correl(torch.from_numpy(x).cuda(), torch.from_numpy(r).cuda()).cpu().numpy()
+        assert_fp64_close(hc, dc, n.bit_length() - 1, "correl host vs device n=%d" % n)
+        z = W.normal(n + 52, 2 * n)
+        zh = z.copy()
+        nr.four1(zh, n, -1)
+        zd = torch.from_numpy(z.copy()).cuda()
+        nr.four1(zd, n, -1)
+        assert_fp64_close(zh, zd.cpu().numpy(), n.bit_length() - 1, "four1 host vs device n=%d" % n)
+
+
 def test_repeat_calls_bit_identical(nr):
     x = W.normal(5, 1 << 16)
     a, b = x.copy(), x.copy()
