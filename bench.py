@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="convlv",
                     choices=["convlv", "four1", "batch", "fourn", "rlft3", "large", "c1"])
-    ap.add_argument("--form", default="fp64", choices=["fp64", "df64", "fp32"])
+    ap.add_argument("--form", default="fp64", choices=["fp64", "df64", "fp32", "tc32"])
     ap.add_argument("--no-forms", action="store_true", help="skip the extra precision forms")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--log2n", type=int, default=0, help="four1 workload size (default 2^24)")
@@ -298,7 +298,7 @@ def run_convlv(args, world, rank, local):
     # ---- other precision forms, same step ----
     forms = {}
     if not args.no_forms and rank == 0:
-        for f in ("df64", "fp32"):
+        for f in ("df64", "fp32", "tc32"):
             if f == form:
                 continue
             for _ in range(3):
@@ -484,7 +484,7 @@ def run_batch(args, world, rank, local):
     nr.set_async(True)
     results = {}
     sample = list(range(0, len(sizes), max(1, len(sizes) // 200)))
-    for form in [args.form] + ([f for f in ("fp64", "df64", "fp32") if f != args.form]
+    for form in [args.form] + ([f for f in ("fp64", "df64", "fp32", "tc32") if f != args.form]
                                if not args.no_forms else []):
         b = nr.FFTBatch(views, form=form)
         buf.copy_(orig)

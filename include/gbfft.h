@@ -48,7 +48,8 @@ typedef enum {
 typedef enum {
   GBFFT_FORM_FP64 = 0,  /* IEEE double throughout (the crate's arithmetic)      */
   GBFFT_FORM_FP32 = 1,  /* IEEE float arithmetic, f64 in and out               */
-  GBFFT_FORM_DF64 = 2   /* double-float (compensated FP32 pairs), f64 in/out    */
+  GBFFT_FORM_DF64 = 2,  /* double-float (compensated FP32 pairs), f64 in/out    */
+  GBFFT_FORM_TC32 = 3   /* FP32, radix-16 stages as 3xTF32 tensor-core products */
 } gbfft_form;
 
 typedef struct {

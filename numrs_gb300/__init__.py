@@ -19,7 +19,8 @@ Arrays are float64: numpy arrays (host memory; copied to and from the GPU
 inside the call) or torch CUDA tensors (device memory; no copies).  In-place
 routines modify their argument.  Every call runs on the GPU; there is no CPU
 path.  ``form`` selects the arithmetic: "fp64" (default, the crate's),
-"fp32", or "df64" (double-float pairs, FP64-class accuracy).
+"fp32", "df64" (double-float pairs, FP64-class accuracy) or "tc32" (FP32 with
+the radix-16 stages as 3xTF32 tensor-core products).
 """
 import ctypes
 

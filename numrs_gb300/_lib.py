@@ -21,7 +21,7 @@ INVALID_ISIGN = 12
 LENGTH_MISMATCH = 13
 ZERO_STD_DEV = 14
 
-FORMS = {"fp64": 0, "fp32": 1, "df64": 2}
+FORMS = {"fp64": 0, "fp32": 1, "df64": 2, "tc32": 3}
 
 
 class Opts(ctypes.Structure):

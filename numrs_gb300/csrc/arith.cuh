@@ -33,6 +33,7 @@ struct alignas(16) f4 { float x, y, z, w; };  // (re.hi, re.lo, im.hi, im.lo)
 // ---------------------------------------------------------------------------
 struct F64 {
   static constexpr int kind = 0;
+  static constexpr bool kTensor = false;
   using real = double;
   struct C { double x, y; };
   using S = d2;
@@ -77,6 +78,7 @@ struct F64 {
 // ---------------------------------------------------------------------------
 struct F32 {
   static constexpr int kind = 1;
+  static constexpr bool kTensor = false;
   using real = float;
   struct C { float x, y; };
   using S = f2;
@@ -190,6 +192,7 @@ __device__ __forceinline__ double df_to_double(df a) { return conv::df2d(a.hi, a
 
 struct DF64 {
   static constexpr int kind = 2;
+  static constexpr bool kTensor = false;
   using real = df;
   struct C { df x, y; };
   using S = f4;
@@ -235,6 +238,14 @@ struct DF64 {
     if (sg < 0) w.y = df_neg(w.y);
     return w;
   }
+};
+
+// ---------------------------------------------------------------------------
+// TC32: FP32 storage and CUDA-core arithmetic, with every radix-16 sub-pass
+// done on the tensor cores as a 3xTF32 DFT-matrix product (tc16.cuh).
+// ---------------------------------------------------------------------------
+struct TC32 : F32 {
+  static constexpr bool kTensor = true;
 };
 
 }  // namespace gbfft

@@ -108,6 +108,9 @@ cudaError_t launch_batch(Form f, int sign, const BatchParams& P, int grid, cudaS
   if (f == FORM_F32)
     return sign > 0 ? launch_batch_t<F32, 1, IO_F2>(P, grid, st)
                     : launch_batch_t<F32, -1, IO_F2>(P, grid, st);
+  if (f == FORM_TC32)
+    return sign > 0 ? launch_batch_t<TC32, 1, IO_F2>(P, grid, st)
+                    : launch_batch_t<TC32, -1, IO_F2>(P, grid, st);
   return sign > 0 ? launch_batch_t<DF64, 1, IO_F4>(P, grid, st)
                   : launch_batch_t<DF64, -1, IO_F4>(P, grid, st);
 }
@@ -117,6 +120,8 @@ int batch_blocks_per_sm(Form f, int sign) {
     return sign > 0 ? occupancy_t<F64, 1, IO_D2>() : occupancy_t<F64, -1, IO_D2>();
   if (f == FORM_F32)
     return sign > 0 ? occupancy_t<F32, 1, IO_F2>() : occupancy_t<F32, -1, IO_F2>();
+  if (f == FORM_TC32)
+    return sign > 0 ? occupancy_t<TC32, 1, IO_F2>() : occupancy_t<TC32, -1, IO_F2>();
   return sign > 0 ? occupancy_t<DF64, 1, IO_F4>() : occupancy_t<DF64, -1, IO_F4>();
 }
 

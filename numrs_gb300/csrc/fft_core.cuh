@@ -18,6 +18,10 @@ constexpr int kEPT = 16;  // complex elements per thread per tile
 
 __device__ __forceinline__ int pidx(int i, int sh) { return i + (i >> sh); }
 
+}  // namespace gbfft
+#include "tc16.cuh"
+namespace gbfft {
+
 // ---------------------------------------------------------------------------
 // Twiddle lookup: w_S^e with sign, S and e < S powers-of-two arithmetic.
 // ---------------------------------------------------------------------------
@@ -295,7 +299,15 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
   for (int k = 0; k < p.nq; ++k) {
     const int lq = p.q[k];
     switch (lq) {
-      case 4: subpass<F, SG, 16>(sm, logR, logNsub, p.tw, tid, T); break;
+      case 4:
+        if constexpr (F::kTensor) {
+          Dft16Frags A;
+          dft16_frags<SG>(reinterpret_cast<const f2*>(p.tw.dense), A);
+          subpass16_tc<SG>(reinterpret_cast<f2*>(sm), logR, logNsub, p.tw, A, tid);
+        } else {
+          subpass<F, SG, 16>(sm, logR, logNsub, p.tw, tid, T);
+        }
+        break;
       case 3: subpass<F, SG, 8>(sm, logR, logNsub, p.tw, tid, T); break;
       case 2: subpass<F, SG, 4>(sm, logR, logNsub, p.tw, tid, T); break;
       default: subpass<F, SG, 2>(sm, logR, logNsub, p.tw, tid, T); break;
@@ -363,5 +375,27 @@ cudaError_t launch_pass_t(const PassParams& p, int threads, cudaStream_t st) {
     default: return launch_pass_one<F, SG, IN, OUT, 32>(p, st);
   }
 }
+
+// All IO combinations of one form and direction (FP64 uses double I/O only).
+// Each (form, direction) is instantiated in its own translation unit so that
+// the library builds in parallel.
+template <class F, int SG>
+cudaError_t dispatch_io(IOType in, IOType out, const PassParams& p, int threads,
+                        cudaStream_t st) {
+  constexpr int S = (F::kind == 2) ? IO_F4 : IO_F2;
+  if (in == IO_D2 && out == IO_D2) return launch_pass_t<F, SG, IO_D2, IO_D2>(p, threads, st);
+  if constexpr (F::kind != 0) {
+    if (in == IO_D2 && out == S) return launch_pass_t<F, SG, IO_D2, S>(p, threads, st);
+    if (in == S && out == IO_D2) return launch_pass_t<F, SG, S, IO_D2>(p, threads, st);
+    if (in == S && out == S) return launch_pass_t<F, SG, S, S>(p, threads, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+#define GBFFT_DECLARE_DISPATCH(FORM)                                                          \
+  extern template cudaError_t dispatch_io<FORM, 1>(IOType, IOType, const PassParams&, int,    \
+                                                   cudaStream_t);                             \
+  extern template cudaError_t dispatch_io<FORM, -1>(IOType, IOType, const PassParams&, int,   \
+                                                    cudaStream_t);
 
 }  // namespace gbfft

@@ -1,0 +1,7 @@
+// fft_df64_m.cu -- Stockham pass kernels in double-float (compensated FP32 pairs), inverse (isign = -1).
+#include "fft_core.cuh"
+
+namespace gbfft {
+template cudaError_t dispatch_io<DF64, -1>(IOType, IOType, const PassParams&, int,
+                                          cudaStream_t);
+}  // namespace gbfft

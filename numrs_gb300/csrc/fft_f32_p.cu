@@ -1,0 +1,7 @@
+// fft_f32_p.cu -- Stockham pass kernels in IEEE float, forward (isign = +1).
+#include "fft_core.cuh"
+
+namespace gbfft {
+template cudaError_t dispatch_io<F32, 1>(IOType, IOType, const PassParams&, int,
+                                          cudaStream_t);
+}  // namespace gbfft

@@ -1,0 +1,7 @@
+// fft_tc32_m.cu -- Stockham pass kernels of the tensor-core form (FP32 data, 3xTF32 radix-16 stages), inverse (isign = -1).
+#include "fft_core.cuh"
+
+namespace gbfft {
+template cudaError_t dispatch_io<TC32, -1>(IOType, IOType, const PassParams&, int,
+                                          cudaStream_t);
+}  // namespace gbfft

@@ -7,7 +7,8 @@
 
 namespace gbfft {
 
-enum Form : int { FORM_F64 = 0, FORM_F32 = 1, FORM_DF64 = 2 };
+enum Form : int { FORM_F64 = 0, FORM_F32 = 1, FORM_DF64 = 2, FORM_TC32 = 3 };
+constexpr int kForms = 4;
 
 // Element types a pass reads or writes in global memory.
 //   IO_D2  interleaved double complex (the caller's layout)
@@ -78,6 +79,8 @@ cudaError_t launch_pass_f32(int sign, IOType in, IOType out, const PassParams& p
                             cudaStream_t st);
 cudaError_t launch_pass_df64(int sign, IOType in, IOType out, const PassParams& p, int threads,
                              cudaStream_t st);
+cudaError_t launch_pass_tc32(int sign, IOType in, IOType out, const PassParams& p, int threads,
+                             cudaStream_t st);
 cudaError_t launch_twiddles(Form f, void* dense, void* partial, cudaStream_t st);
 
 // spectral / real-transform kernels (spectral.cu)
@@ -127,6 +130,7 @@ cudaError_t launch_cosft2_inv_post(const double* w, double* y, long long n, Twid
 cudaError_t launch_trig_scan(int kind, double* y, long long n, double* partial, double* work,
                              cudaStream_t st);
 cudaError_t launch_scale(double* data, long long count, double s, cudaStream_t st);
+cudaError_t launch_set_lines(const void** dst, const void* a, const void* b, cudaStream_t st);
 // Normalised correlation helpers (src/Correlation.rs:189-270).
 cudaError_t launch_correl_direct_centered(const double* a, const double* b, double* out,
                                           long long n, double ma, double mb, double norm,

@@ -41,8 +41,8 @@ struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;  // library stream
   cudaStream_t cur = nullptr;     // stream of the call in progress
-  void* tw_dense[3] = {nullptr, nullptr, nullptr};
-  void* tw_part[3] = {nullptr, nullptr, nullptr};
+  void* tw_dense[kForms] = {nullptr, nullptr, nullptr, nullptr};
+  void* tw_part[kForms] = {nullptr, nullptr, nullptr, nullptr};
   DevBuf scratch;   // Stockham ping-pong buffer
   DevBuf work;      // spectral working set (two n-real lines)
   DevBuf stage_a;   // device copies of host arguments
@@ -134,6 +134,7 @@ int init_locked(int device) {
 }
 
 int tables(Form f, Twiddles& tw) {
+  if (f == FORM_TC32) f = FORM_F32;  // the tensor-core form uses the FP32 tables
   if (!g.tw_dense[f]) {
     size_t esz = (f == FORM_F32) ? 8 : 16;
     CK(cudaMalloc(&g.tw_dense[f], kDenseEntries * esz));
@@ -182,7 +183,9 @@ struct ProfScope {
   }
 };
 
-IOType scratch_io(Form f) { return f == FORM_F64 ? IO_D2 : (f == FORM_F32 ? IO_F2 : IO_F4); }
+IOType scratch_io(Form f) {
+  return f == FORM_F64 ? IO_D2 : (f == FORM_DF64 ? IO_F4 : IO_F2);
+}
 
 // ---------------------------------------------------------------------------
 // Axis plan: the Stockham pass schedule for `nlines` lines of length L along
@@ -302,6 +305,7 @@ int launch_pass(Form f, int sign, IOType in, IOType out, const PassParams& p, in
   ProfScope ps(PK_PASS, pts * (double)(io_bytes(in) + io_bytes(out)), 5.0 * pts * p.logR);
   if (f == FORM_F64) e = launch_pass_f64(sign, in, out, p, threads, g.cur);
   else if (f == FORM_F32) e = launch_pass_f32(sign, in, out, p, threads, g.cur);
+  else if (f == FORM_TC32) e = launch_pass_tc32(sign, in, out, p, threads, g.cur);
   else e = launch_pass_df64(sign, in, out, p, threads, g.cur);
   g.launches++;
   if (e != cudaSuccess)
@@ -393,7 +397,7 @@ struct Call {
 };
 
 int check_form(const Call& c) {
-  if (c.o->form < 0 || c.o->form > 2) return fail(GBFFT_INVALID_ARG, "unknown form %d", c.o->form);
+  if (c.o->form < 0 || c.o->form >= kForms) return fail(GBFFT_INVALID_ARG, "unknown form %d", c.o->form);
   return GBFFT_OK;
 }
 
@@ -717,7 +721,8 @@ int spectral_direct(Form f, int kind, const double* a, const double* b, long lon
     lines[1] = w + n;
   }
   TRY(ensure(g.ptrtab, 64));
-  CK(cudaMemcpyAsync(g.ptrtab.p, lines, sizeof lines, cudaMemcpyHostToDevice, g.cur));
+  CK(launch_set_lines((const void**)g.ptrtab.p, lines[0], lines[1], g.cur));
+  g.launches++;
   TRY(run_axis_io(f, 1, axis_plan(nh, 1, 2, 0, nh), nullptr, (const void* const*)g.ptrtab.p, w));
   {
     ProfScope ps(PK_SPECTRAL, 3.0 * n * 8);

@@ -151,7 +151,7 @@ cudaError_t launch_realft_twist(Form f, int isign, double* data, long long n, lo
   (isign > 0 ? (k_realft_twist<FT, 1><<<blocks, 256, 0, st>>>(data, n, batch, dist, tw)) \
              : (k_realft_twist<FT, -1><<<blocks, 256, 0, st>>>(data, n, batch, dist, tw)))
   if (f == FORM_F64) TW_LAUNCH(F64);
-  else if (f == FORM_F32) TW_LAUNCH(F32);
+  else if (f == FORM_F32 || f == FORM_TC32) TW_LAUNCH(F32);
   else TW_LAUNCH(DF64);
 #undef TW_LAUNCH
   return cudaGetLastError();
@@ -257,7 +257,7 @@ cudaError_t launch_spectral_product(Form f, int kind, const double* a, const dou
     default: k_spectral<FT, 2><<<blocks, 256, 0, st>>>(a, b, out, n, tw); break;           \
   }
   if (f == FORM_F64) { SP_LAUNCH(F64) }
-  else if (f == FORM_F32) { SP_LAUNCH(F32) }
+  else if (f == FORM_F32 || f == FORM_TC32) { SP_LAUNCH(F32) }
   else { SP_LAUNCH(DF64) }
 #undef SP_LAUNCH
   return cudaGetLastError();
@@ -523,7 +523,7 @@ cudaError_t launch_rlft3_twist(Form f, int isign, double* data, double* speq, lo
   (isign > 0 ? (k_rlft3_twist<FT, 1><<<blocks, 256, 0, st>>>(data, speq, nn1, nn2, nn3, tw)) \
              : (k_rlft3_twist<FT, -1><<<blocks, 256, 0, st>>>(data, speq, nn1, nn2, nn3, tw)))
   if (f == FORM_F64) R3_LAUNCH(F64);
-  else if (f == FORM_F32) R3_LAUNCH(F32);
+  else if (f == FORM_F32 || f == FORM_TC32) R3_LAUNCH(F32);
   else R3_LAUNCH(DF64);
 #undef R3_LAUNCH
   return cudaGetLastError();
@@ -536,6 +536,18 @@ __global__ void k_scale(double* d, long long count, double s) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
        i += (long long)gridDim.x * blockDim.x)
     d[i] *= s;
+}
+
+// Writes two line pointers into device memory in stream order (a copy from
+// pageable host memory would first wait for the stream to drain).
+__global__ void k_set_lines(const void** dst, const void* a, const void* b) {
+  dst[0] = a;
+  dst[1] = b;
+}
+
+cudaError_t launch_set_lines(const void** dst, const void* a, const void* b, cudaStream_t st) {
+  k_set_lines<<<1, 1, 0, st>>>(dst, a, b);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_scale(double* data, long long count, double s, cudaStream_t st) {

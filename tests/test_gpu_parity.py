@@ -2,7 +2,7 @@
 
 Bars (written into each check):
   FP64 and DF64 forms: rel-L2 <= 1e-12 and max-abs <= 1e-12 * ||X_ref||_inf * log2 N
-  FP32 form:           rel-L2 <= 1e-6
+  FP32 and tensor-core (3xTF32) forms: rel-L2 <= 1e-6
 """
 import os
 
@@ -16,7 +16,7 @@ from conftest import rel_l2, assert_fp64_close
 pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden", "golden.npz")
-FORMS = ["fp64", "df64", "fp32"]
+FORMS = ["fp64", "df64", "fp32", "tc32"]
 
 
 @pytest.fixture(scope="module")
@@ -28,9 +28,9 @@ def nr():
 
 
 def check(got, ref, log2n, form, what=""):
-    if form == "fp32":
+    if form in ("fp32", "tc32"):
         e = rel_l2(got, ref)
-        assert e <= 1e-6, "%s fp32 rel-L2 %.3e > 1e-6" % (what, e)
+        assert e <= 1e-6, "%s %s rel-L2 %.3e > 1e-6" % (what, form, e)
     else:
         assert_fp64_close(got, ref, log2n, "%s %s" % (what, form))
 
@@ -123,25 +123,25 @@ def test_fft_batch_uneven(nr, form):
 @pytest.mark.parametrize("form", FORMS)
 def test_fft_batch_device_graph_replay(nr, form):
     """Device tensors through the persistent batched launch: the first call
-    builds and captures the plan, the second replays the graph; both must match
-    the oracle, including 2^13 / 2^14 sizes (two passes with completion
-    counters) and a size above the persistent limit."""
+    builds and captures the plan, a repeated call replays the graph, a call in
+    the other direction rebuilds it; every call is checked against the oracle,
+    including 2^13 / 2^14 sizes (two passes with completion counters) and a
+    size above the persistent limit."""
     torch = pytest.importorskip("torch")
     sizes = [64, 8192, 128, 16384, 4096, 1 << 21, 256, 16384, 2, 1, 8192, 512] * 3
     data = [W.normal(400 + i, 2 * s) for i, s in enumerate(sizes)]
     tens = [torch.from_numpy(a.copy()).cuda() for a in data]
     b = nr.FFTBatch(tens, form=form)
-    b.run(1)
-    b.run(-1)  # round trip: second call with the other sign rebuilds the plan
-    b.run(1)   # same sign again: replay of a cached graph is exercised below
-    b.run(1)
-    torch.cuda.synchronize()
-    for a, t, s in zip(data, tens, sizes):
-        ref = a.copy()
-        for sg in (1, -1, 1, 1):
+    for sg in (1, 1, -1, 1):
+        for t, a in zip(tens, data):
+            t.copy_(torch.from_numpy(a))
+        b.run(sg)
+        torch.cuda.synchronize()
+        for a, t, s in zip(data, tens, sizes):
+            ref = a.copy()
             O.four1(ref, s, sg)
-        ref = ref * 1.0
-        check(t.cpu().numpy(), ref, max(1, s.bit_length() - 1), form, "batch replay nn=%d" % s)
+            check(t.cpu().numpy(), ref, max(1, s.bit_length() - 1), form,
+                  "batch nn=%d isign=%d" % (s, sg))
 
 
 @pytest.mark.parametrize("form", FORMS)
