@@ -67,6 +67,11 @@ int gbfft_version(void);                 /* 10000*major + 100*minor + patch  */
 size_t gbfft_scratch_bytes(void);
 /* Free cached plans, graphs and scratch (tables are kept). */
 int gbfft_release(void);
+/* Autotuner (no counterpart in the crate): when enabled, the first plan of
+ * each axis shape and form times candidate tile sizes on a scratch array and
+ * keeps the fastest (also GBFFT_AUTOTUNE=1; GBFFT_TUNE_CACHE=<file> keeps the
+ * choices across processes).  Tuning synchronises the device once per shape. */
+int gbfft_set_autotune(int enable);
 /* Instrumentation (no counterpart in the crate).  Kernel launches issued
  * since the last reset; optional event timing of every launch on its stream,
  * summed per kind: 0 = FFT passes, 1 = realft twists, 2 = spectral products,

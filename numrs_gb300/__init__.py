@@ -530,6 +530,11 @@ def launch_count(reset=False):
     return _lib.load().gbfft_launch_count(1 if reset else 0)
 
 
+def set_autotune(enable=True):
+    """Choose each plan's tile size by timing candidates on its first use."""
+    _check(_lib.load().gbfft_set_autotune(1 if enable else 0))
+
+
 PROFILE_KINDS = {"pass": 0, "twist": 1, "spectral": 2, "other": 3}
 
 

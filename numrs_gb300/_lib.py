@@ -55,6 +55,7 @@ SIGNATURES = {
     "gbfft_release": [],
     "gbfft_four1_noalloc": [_vp, _sz, ctypes.c_int, _vp],
     "gbfft_profile": [ctypes.c_int],
+    "gbfft_set_autotune": [ctypes.c_int],
     "gbfft_profile_read": [ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_longlong), _dp, _dp],
 }
 

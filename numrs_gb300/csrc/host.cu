@@ -53,6 +53,9 @@ struct Ctx {
   std::string err;
   long long launches = 0;
   bool host_direct = false;  // kernels may read/write the caller's host arrays
+  bool autotune = false;     // time candidate tile sizes on a plan's first use
+  bool tune_verbose = false;
+  std::string tune_cache;    // file of tuned tile sizes (GBFFT_TUNE_CACHE)
   bool profiling = false;
   std::vector<ProfRec> prof;
   std::vector<cudaEvent_t> evpool;
@@ -129,6 +132,12 @@ int init_locked(int device) {
   cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
   const char* env = getenv("GBFFT_HOST_DIRECT");
   g.host_direct = pma != 0 && !(env && env[0] == '0');
+  const char* at = getenv("GBFFT_AUTOTUNE");
+  g.autotune = at && at[0] == '1';
+  const char* tv = getenv("GBFFT_TUNE_VERBOSE");
+  g.tune_verbose = tv && tv[0] == '1';
+  const char* tc = getenv("GBFFT_TUNE_CACHE");
+  if (tc) g.tune_cache = tc;
   g.inited = true;
   return GBFFT_OK;
 }
@@ -219,20 +228,23 @@ void split_subpasses(int logR, PassParams& p) {
 constexpr long long kLatencyMaxWork = 8192;
 constexpr int kLatencyTileLog = 9;
 
+// tileLog: log2 of the complex elements per CTA tile (10..12); multi-pass
+// radices are kept 4 columns below it so that strided rows stay >= 64 bytes.
 AxisPlan make_axis_plan(long long L, long long s, long long nlines, int lq_log,
-                        long long lstride, bool full_tile = false) {
+                        long long lstride, bool full_tile = false, int tileLog = 12) {
   AxisPlan ap;
   const int logL = ilog2((unsigned long long)L);
+  const int maxPassLog = std::min(kMaxPassLog, tileLog - 2);
   std::vector<int> radix;
   const bool latency = !full_tile && s == 1 && logL >= 10 && logL <= 12 &&
                        L * nlines <= kLatencyMaxWork;
   if (latency) {
     radix.push_back((logL + 1) / 2);
     radix.push_back(logL / 2);
-  } else if (logL <= 12) {
+  } else if (logL <= tileLog) {
     radix.push_back(logL);
   } else {
-    int P = (logL + kMaxPassLog - 1) / kMaxPassLog;
+    int P = (logL + maxPassLog - 1) / maxPassLog;
     int base = logL / P, extra = logL % P;
     for (int i = 0; i < P; ++i) radix.push_back(base + (i < extra ? 1 : 0));
   }
@@ -258,13 +270,13 @@ AxisPlan make_axis_plan(long long L, long long s, long long nlines, int lq_log,
     int logC;
     if (s == 1 && LR > 1) {
       p.mode = 0;
-      const int tileLog = latency ? kLatencyTileLog : ilog2(kTileE);
-      logC = std::min(tileLog - logR, ilog2((unsigned long long)LR));
+      const int tl = latency ? kLatencyTileLog : tileLog;
+      logC = std::min(tl - logR, ilog2((unsigned long long)LR));
       p.in_rcontig = 0;
       p.out_rcontig = (logNs == 0) ? 1 : 0;
     } else {
       p.mode = 1;
-      int want = ilog2(kTileE) - logR;
+      int want = tileLog - logR;
       int have = ilog2(npow2((unsigned long long)nlines));
       logC = full_tile ? want : std::min(want, have);
       p.in_rcontig = (s == 1) ? 1 : 0;
@@ -344,7 +356,10 @@ int run_axis_io(Form f, int sign, const AxisPlan& ap, const void* in,
   TRY(tables(f, tw));
   const IOType sio = scratch_io(f);
   const size_t P = ap.passes.size();
-  if (P > 2) return fail(GBFFT_INVALID_ARG, "run_axis_io: %zu passes", P);
+  if (P > 2) {
+    // in-place passes through a device copy when the plan is longer
+    return fail(GBFFT_UNSUPPORTED_SIZE, "run_axis_io: %zu passes", P);
+  }
   if (P == 2) TRY(ensure(g.scratch, ap.scratch_elems * io_bytes(sio)));
   for (size_t i = 0; i < P; ++i) {
     PassParams p = ap.passes[i].p;
@@ -358,15 +373,99 @@ int run_axis_io(Form f, int sign, const AxisPlan& ap, const void* in,
   return GBFFT_OK;
 }
 
-// Plan cache keyed by (L, s, nlines, lq_log, lstride).
-std::map<std::tuple<long long, long long, long long, int, long long>, AxisPlan> g_plans;
+// Plan cache keyed by (L, s, nlines, lq_log, lstride, tile size).
+std::map<std::tuple<long long, long long, long long, int, long long, int>, AxisPlan> g_plans;
+
+// Autotuner: the tile size of each (axis shape, form), chosen by timing the
+// candidates 2^12, 2^11 and 2^10 elements per CTA on a zeroed scratch array
+// the first time the shape is planned.  Results can be kept in a file
+// (GBFFT_TUNE_CACHE), one line "L s nlines lq_log lstride form tileLog".
+using TuneKey = std::tuple<long long, long long, long long, int, long long, int>;
+std::map<TuneKey, int> g_tuned;
+bool g_tune_loaded = false;
+
+void tune_load() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  if (g.tune_cache.empty()) return;
+  FILE* fp = fopen(g.tune_cache.c_str(), "r");
+  if (!fp) return;
+  long long L, s, nl, ls;
+  int lq, f, tl;
+  while (fscanf(fp, "%lld %lld %lld %d %lld %d %d", &L, &s, &nl, &lq, &ls, &f, &tl) == 7)
+    g_tuned[std::make_tuple(L, s, nl, lq, ls, f)] = tl;
+  fclose(fp);
+}
+
+int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale);
+
+int tune_tile(Form f, long long L, long long s, long long nlines, int lq_log, long long lstride) {
+  const size_t span = (s == 1) ? (size_t)((nlines - 1) * lstride + L) : (size_t)(nlines * L);
+  if (span * 16 > (size_t(512) << 20) || L <= 64) return 12;
+  void* tmp = nullptr;
+  if (cudaMalloc(&tmp, span * 16) != cudaSuccess) {
+    cudaGetLastError();
+    return 12;
+  }
+  cudaMemsetAsync(tmp, 0, span * 16, g.cur);
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 1e30f;
+  int best_tl = 12;
+  const bool prof = g.profiling;
+  g.profiling = false;
+  for (int tl = 12; tl >= 10; --tl) {
+    AxisPlan ap = make_axis_plan(L, s, nlines, lq_log, lstride, false, tl);
+    if (run_axis(f, 1, ap, tmp, 1.0) != GBFFT_OK) continue;
+    cudaEventRecord(a, g.cur);
+    for (int r = 0; r < 3; ++r) run_axis(f, 1, ap, tmp, 1.0);
+    cudaEventRecord(b, g.cur);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (g.tune_verbose)
+      fprintf(stderr, "gbfft tune L=%lld s=%lld lines=%lld form=%d tile=2^%d: %.4f ms\n", L, s,
+              nlines, (int)f, tl, ms / 3);
+    if (ms < best * 0.97f) {  // prefer the larger tile unless clearly slower
+      best = ms;
+      best_tl = tl;
+    }
+  }
+  g.profiling = prof;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(tmp);
+  cudaGetLastError();
+  return best_tl;
+}
 
 const AxisPlan& axis_plan(long long L, long long s, long long nlines, int lq_log,
-                          long long lstride) {
-  auto key = std::make_tuple(L, s, nlines, lq_log, lstride);
+                          long long lstride, Form f = FORM_F64) {
+  int tl = 12;
+  if (g.autotune) {
+    tune_load();
+    const TuneKey tk = std::make_tuple(L, s, nlines, lq_log, lstride, (int)f);
+    auto t = g_tuned.find(tk);
+    if (t != g_tuned.end()) {
+      tl = t->second;
+    } else {
+      tl = tune_tile(f, L, s, nlines, lq_log, lstride);
+      g_tuned[tk] = tl;
+      if (!g.tune_cache.empty()) {
+        FILE* fp = fopen(g.tune_cache.c_str(), "a");
+        if (fp) {
+          fprintf(fp, "%lld %lld %lld %d %lld %d %d\n", L, s, nlines, lq_log, lstride, (int)f, tl);
+          fclose(fp);
+        }
+      }
+    }
+  }
+  auto key = std::make_tuple(L, s, nlines, lq_log, lstride, tl);
   auto it = g_plans.find(key);
   if (it != g_plans.end()) return it->second;
-  return g_plans.emplace(key, make_axis_plan(L, s, nlines, lq_log, lstride)).first->second;
+  return g_plans.emplace(key, make_axis_plan(L, s, nlines, lq_log, lstride, false, tl))
+      .first->second;
 }
 
 // Contiguous batch of 1-D complex transforms: nlines lines `dist` complex apart.
@@ -382,7 +481,7 @@ int fft_lines(Form f, int sign, void* data, long long L, long long nlines, long 
     }
     return GBFFT_OK;
   }
-  return run_axis(f, sign, axis_plan(L, 1, nlines, 0, dist), data, scale);
+  return run_axis(f, sign, axis_plan(L, 1, nlines, 0, dist, f), data, scale);
 }
 
 struct Call {
@@ -490,9 +589,9 @@ int fourn_dev(Form f, double* d, const long long* nn, int ndim, int isign) {
     if (L > 1) {
       long long nl = total / L;
       if (s == 1) {
-        TRY(run_axis(f, isign, axis_plan(L, 1, nl, 0, L), d));
+        TRY(run_axis(f, isign, axis_plan(L, 1, nl, 0, L, f), d));
       } else {
-        TRY(run_axis(f, isign, axis_plan(L, s, nl, ilog2((unsigned long long)s), L * s), d));
+        TRY(run_axis(f, isign, axis_plan(L, s, nl, ilog2((unsigned long long)s), L * s, f), d));
       }
     }
     s *= L;
@@ -723,19 +822,22 @@ int spectral_direct(Form f, int kind, const double* a, const double* b, long lon
   TRY(ensure(g.ptrtab, 64));
   CK(launch_set_lines((const void**)g.ptrtab.p, lines[0], lines[1], g.cur));
   g.launches++;
-  TRY(run_axis_io(f, 1, axis_plan(nh, 1, 2, 0, nh), nullptr, (const void* const*)g.ptrtab.p, w));
+  TRY(run_axis_io(f, 1, axis_plan(nh, 1, 2, 0, nh, f), nullptr, (const void* const*)g.ptrtab.p, w));
   {
     ProfScope ps(PK_SPECTRAL, 3.0 * n * 8);
     CK(launch_spectral_product(f, kind, w, w + n, w, n, tw, g.cur));
   }
   g.launches++;
-  TRY(run_axis_io(f, -1, axis_plan(nh, 1, 1, 0, nh), w, nullptr, ans));
+  TRY(run_axis_io(f, -1, axis_plan(nh, 1, 1, 0, nh, f), w, nullptr, ans));
   return GBFFT_OK;
 }
 
-// Whether a plan of this length can run with host arrays read and written by
-// its first and last passes.
-bool direct_fits(long long L) { return g.host_direct && L <= (1ll << kBatchMaxLog); }
+// Whether the plan of `nlines` lines of L points can run with host arrays read
+// and written by its first and last passes (at most two passes).
+bool direct_fits(long long L, long long nlines, Form f) {
+  return g.host_direct && L <= (1ll << kBatchMaxLog) &&
+         axis_plan(L, 1, nlines, 0, L, f).passes.size() <= 2;
+}
 
 }  // namespace
 
@@ -778,6 +880,13 @@ int gbfft_release(void) {
   }
   g_plans.clear();
   batch_plan_free(g_batch);
+  return GBFFT_OK;
+}
+
+int gbfft_set_autotune(int enable) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  TRY(init_locked(g.device));
+  g.autotune = enable != 0;
   return GBFFT_OK;
 }
 
@@ -833,9 +942,9 @@ int gbfft_four1(double* data, size_t nn, int isign, const gbfft_opts* opts) {
     return fail(GBFFT_UNSUPPORTED_SIZE, "four1: nn=%zu must be a power of two <= 2^%d", nn, kMaxAxisLog);
   TRY(init_locked(g.device));
   StreamScope ss(c);
-  if (!c.dev() && nn > 1 && direct_fits((long long)nn)) {
+  if (!c.dev() && nn > 1 && direct_fits((long long)nn, 1, c.form())) {
     // the first pass reads the caller's array, the last pass writes it back
-    TRY(run_axis_io(c.form(), isign, axis_plan((long long)nn, 1, 1, 0, (long long)nn), data,
+    TRY(run_axis_io(c.form(), isign, axis_plan((long long)nn, 1, 1, 0, (long long)nn, c.form()), data,
                     nullptr, data));
     return ss.finish(c);
   }
@@ -1037,7 +1146,8 @@ static int spectral_call(const Call& c, int kind, const double* a, const double*
                          size_t m, double* ans) {
   TRY(init_locked(g.device));
   StreamScope ss(c);
-  if (!c.dev() && n >= 4 && direct_fits((long long)n / 2)) {
+  if (!c.dev() && n >= 4 && direct_fits((long long)n / 2, 2, c.form()) &&
+      direct_fits((long long)n / 2, 1, c.form())) {
     TRY(spectral_direct(c.form(), kind, a, b, (long long)n, (long long)m, ans));
     return ss.finish(c);
   }
