@@ -32,5 +32,9 @@ cudaError_t launch_batch(Form f, int sign, const BatchParams& P, int grid, cudaS
 // Resident CTAs per SM; also raises the kernel's shared memory limit, so it
 // is called before the launch is captured.
 int batch_blocks_per_sm(Form f, int sign);
+// Prefetching variant (FP32, TC32, DF64 forms; every caller array 16-byte
+// aligned): bulk copies of the next tile overlap the current tile's compute.
+cudaError_t launch_batch_pf(Form f, int sign, const BatchParams& P, int grid, cudaStream_t st);
+int batch_pf_blocks_per_sm(Form f, int sign);
 
 }  // namespace gbfft

@@ -221,80 +221,56 @@ template <> struct IOElem<IO_D2> { using T = d2; };
 template <> struct IOElem<IO_F2> { using T = f2; };
 template <> struct IOElem<IO_F4> { using T = f4; };
 
-template <class F, int SG, int IN, int OUT, int T, bool L2_ONLY>
-__device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
-                                          typename F::S* sm, int tid) {
+// tile index -> first line and first column j of the tile
+__device__ __forceinline__ void tile_origin(const PassParams& p, long long tile, long long& line0,
+                                            long long& j0) {
+  const int logLR = p.logL - p.logR;
+  if (p.mode == 0) {
+    const int logTpl = logLR - p.logC;  // tiles per line
+    line0 = tile >> logTpl;
+    j0 = (tile & ((1ll << logTpl) - 1)) << p.logC;
+  } else {
+    const long long ng = (p.nlines + (1ll << p.logC) - 1) >> p.logC;
+    j0 = tile / ng;
+    line0 = (tile - j0 * ng) << p.logC;
+  }
+}
+
+// (column, row) of tile element e in the load order: contiguous along r when
+// the tile's columns are contiguous runs in memory, along c otherwise.
+__device__ __forceinline__ void elem_cr(int e, int rcontig, int logR, int logC, int& c, int& r) {
+  if (rcontig) { r = e & ((1 << logR) - 1); c = e >> logR; }
+  else { c = e & ((1 << logC) - 1); r = e >> logC; }
+}
+
+// Element e of the tile (raw value from global memory or a staging buffer):
+// convert, apply the inter-pass twiddle, store into the padded tile.
+template <class F, int SG, int IN>
+__device__ __forceinline__ void stage_elem(const PassParams& p, long long line0, long long j0,
+                                           int e, const typename IOElem<IN>::T& rawv,
+                                           typename F::S* sm) {
   using C = typename F::C;
-  using IE = typename IOElem<IN>::T;
+  int c, r;
+  elem_cr(e, p.in_rcontig, p.logR, p.logC, c, r);
+  const long long line = (p.mode == 0) ? line0 : line0 + c;
+  C v = (line < p.nlines) ? gload<F, IN>(&rawv, 0) : F::from_d(0.0, 0.0);
+  if (p.logNs > 0) {
+    const long long j = (p.mode == 0) ? j0 + c : j0;
+    const long long jm = j & (p.Ns - 1);
+    if (jm != 0 && r != 0) v = F::mul(v, twiddle<F>(p.tw, p.logNs + p.logR, jm * r, SG));
+  }
+  sm[pidx((c << p.logR) + r, F::kPadShift)] = F::to_s(v);
+}
+
+// The R-point DFTs of the tile's columns, then the store at the autosorted
+// positions.  Starts after a barrier that made the staged tile visible.
+template <class F, int SG, int OUT, int T>
+__device__ __forceinline__ void tile_compute_store(const PassParams& p, long long line0,
+                                                   long long j0, typename F::S* sm, int tid) {
+  using C = typename F::C;
   using OE = typename IOElem<OUT>::T;
   constexpr int sh = F::kPadShift;
   const int logR = p.logR, logC = p.logC;
-  const int R = 1 << logR;
-  const int Cn = 1 << logC;
-
-  // tile -> (first line, first j)
-  long long line0, j0;
-  const int logLR = p.logL - logR;  // log2(L/R)
-  if (p.mode == 0) {
-    const int logTpl = logLR - logC;  // tiles per line
-    line0 = tile >> logTpl;
-    j0 = (tile & ((1ll << logTpl) - 1)) << logC;
-  } else {
-    const long long ng = (p.nlines + Cn - 1) >> logC;
-    j0 = tile / ng;
-    line0 = (tile - j0 * ng) << logC;
-  }
-  const long long lqmask = (1ll << p.lq_log) - 1;
-
-  // ---- load tile: global -> (twiddle) -> shared ----
-  // All sixteen loads of a thread are issued before any is used, so that each
-  // SM keeps enough bytes in flight to cover the memory latency.
-  IE raw[kEPT];
-#pragma unroll
-  for (int k = 0; k < kEPT; ++k) {
-    const int e = tid + k * T;
-    int c, r;
-    if (p.in_rcontig) { r = e & (R - 1); c = e >> logR; }
-    else { c = e & (Cn - 1); r = e >> logC; }
-    long long line = line0, j = j0;
-    if (p.mode == 0) j += c; else line += c;
-    if (line < p.nlines) {
-      const IE* base = p.in_ptrs
-          ? reinterpret_cast<const IE*>(p.in_ptrs[line])
-          : reinterpret_cast<const IE*>(p.in) + ((line >> p.lq_log) * p.lstride + (line & lqmask));
-      const IE* src = base + (j + ((long long)r << logLR)) * p.s;
-      if constexpr (L2_ONLY) {
-        if constexpr (sizeof(IE) == 8) {
-          float2 t = __ldcg(reinterpret_cast<const float2*>(src));
-          memcpy(&raw[k], &t, 8);
-        } else {
-          float4 t = __ldcg(reinterpret_cast<const float4*>(src));
-          memcpy(&raw[k], &t, 16);
-        }
-      } else {
-        raw[k] = *src;
-      }
-    } else {
-      memset(&raw[k], 0, sizeof(IE));
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < kEPT; ++k) {
-    const int e = tid + k * T;
-    int c, r;
-    if (p.in_rcontig) { r = e & (R - 1); c = e >> logR; }
-    else { c = e & (Cn - 1); r = e >> logC; }
-    C v = gload<F, IN>(&raw[k], 0);
-    if (p.logNs > 0) {
-      const long long j = (p.mode == 0) ? j0 + c : j0;
-      const long long jm = j & (p.Ns - 1);
-      if (jm != 0 && r != 0) v = F::mul(v, twiddle<F>(p.tw, p.logNs + logR, jm * r, SG));
-    }
-    sm[pidx((c << logR) + r, sh)] = F::to_s(v);
-  }
-  __syncthreads();
-
-  // ---- R-point DFTs of the C columns ----
   int logNsub = 0;
   for (int k = 0; k < p.nq; ++k) {
     const int lq = p.q[k];
@@ -314,14 +290,12 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
     }
     logNsub += lq;
   }
-
-  // ---- store tile: shared -> global at the autosorted positions ----
+  const long long lqmask = (1ll << p.lq_log) - 1;
 #pragma unroll 4
   for (int k = 0; k < kEPT; ++k) {
     const int e = tid + k * T;
     int c, r;
-    if (p.out_rcontig) { r = e & (R - 1); c = e >> logR; }
-    else { c = e & (Cn - 1); r = e >> logC; }
+    elem_cr(e, p.out_rcontig, logR, logC, c, r);
     long long line = line0, j = j0;
     if (p.mode == 0) j += c; else line += c;
     if (line >= p.nlines) continue;
@@ -333,6 +307,62 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
     const long long jd = ((j >> p.logNs) << (p.logNs + logR)) + (j & (p.Ns - 1));
     gstore<F, OUT>(base, (jd + ((long long)r << p.logNs)) * p.s, v);
   }
+}
+
+// Address of tile element e in global memory (input side).
+template <int IN>
+__device__ __forceinline__ const typename IOElem<IN>::T* elem_src(const PassParams& p,
+                                                                  long long line0, long long j0,
+                                                                  int e, bool& valid) {
+  using IE = typename IOElem<IN>::T;
+  int c, r;
+  elem_cr(e, p.in_rcontig, p.logR, p.logC, c, r);
+  long long line = line0, j = j0;
+  if (p.mode == 0) j += c; else line += c;
+  valid = line < p.nlines;
+  if (!valid) return nullptr;
+  const long long lqmask = (1ll << p.lq_log) - 1;
+  const IE* base = p.in_ptrs
+      ? reinterpret_cast<const IE*>(p.in_ptrs[line])
+      : reinterpret_cast<const IE*>(p.in) + ((line >> p.lq_log) * p.lstride + (line & lqmask));
+  return base + (j + ((long long)r << (p.logL - p.logR))) * p.s;
+}
+
+// One full tile from global memory.  All sixteen loads of a thread are issued
+// before any is used, so that each SM keeps enough bytes in flight to cover
+// the memory latency.  L2_ONLY loads bypass L1 (data written by other CTAs of
+// the same launch).
+template <class F, int SG, int IN, int OUT, int T, bool L2_ONLY>
+__device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
+                                          typename F::S* sm, int tid) {
+  using IE = typename IOElem<IN>::T;
+  long long line0, j0;
+  tile_origin(p, tile, line0, j0);
+  IE raw[kEPT];
+#pragma unroll
+  for (int k = 0; k < kEPT; ++k) {
+    bool valid;
+    const IE* src = elem_src<IN>(p, line0, j0, tid + k * T, valid);
+    if (valid) {
+      if constexpr (L2_ONLY) {
+        if constexpr (sizeof(IE) == 8) {
+          float2 t = __ldcg(reinterpret_cast<const float2*>(src));
+          memcpy(&raw[k], &t, 8);
+        } else {
+          float4 t = __ldcg(reinterpret_cast<const float4*>(src));
+          memcpy(&raw[k], &t, 16);
+        }
+      } else {
+        raw[k] = *src;
+      }
+    } else {
+      memset(&raw[k], 0, sizeof(IE));
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kEPT; ++k) stage_elem<F, SG, IN>(p, line0, j0, tid + k * T, raw[k], sm);
+  __syncthreads();
+  tile_compute_store<F, SG, OUT, T>(p, line0, j0, sm, tid);
 }
 
 // One CTA per tile.  Two 256-thread CTAs fit on an SM (registers capped at

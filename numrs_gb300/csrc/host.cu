@@ -629,6 +629,7 @@ struct BatchPlan {
   DevBuf ranges, ptrtab, done, flags, scratch;
   BatchParams P;
   int grid = 0;
+  bool prefetch = false;  // bulk-copy prefetching kernel
   cudaGraphExec_t exec = nullptr;
   long long launches_per_call = 0;
   bool valid = false;
@@ -739,7 +740,14 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
   b.P.spin_limit = 1u << 24;
   int dev_sms = 0;
   CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, g.device));
-  int per = batch_blocks_per_sm(f, sign);
+  // The prefetching kernel needs 16-byte aligned caller arrays (bulk copies);
+  // the FP64 form is FP64-pipe bound and gains nothing from it.
+  bool aligned = true;
+  for (size_t i = 0; i < count; ++i)
+    if (((uintptr_t)dptrs[i]) & 15u) aligned = false;
+  const char* pfenv = getenv("GBFFT_BATCH_PREFETCH");
+  b.prefetch = f != FORM_F64 && aligned && !(pfenv && pfenv[0] == '0');
+  int per = b.prefetch ? batch_pf_blocks_per_sm(f, sign) : batch_blocks_per_sm(f, sign);
   if (per < 1) per = 1;
   b.grid = (int)std::min<long long>((long long)dev_sms * per, std::max<long long>(item, 1));
   // capture [reset counters, persistent launch] on the library stream
@@ -748,7 +756,9 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
   cudaMemsetAsync(b.flags.p, 0, 16, g.stream);
   cudaMemsetAsync(b.done.p, 0, std::max<size_t>(count, 1) * sizeof(unsigned int), g.stream);
   cudaError_t le = cudaSuccess;
-  if (item > 0) le = launch_batch(f, sign, b.P, b.grid, g.stream);
+  if (item > 0)
+    le = b.prefetch ? launch_batch_pf(f, sign, b.P, b.grid, g.stream)
+                    : launch_batch(f, sign, b.P, b.grid, g.stream);
   cudaError_t ce = cudaStreamEndCapture(g.stream, &graph);
   if (le != cudaSuccess || ce != cudaSuccess) {
     if (graph) cudaGraphDestroy(graph);
