@@ -22,7 +22,8 @@
 namespace gbfft {
 
 template <class F, int SG, int SIO>
-__global__ void __launch_bounds__(256, 2) k_batch(BatchParams P) {
+__global__ void __launch_bounds__(256, (F::kind == 1 && !F::kTensor ? 3 : 2))
+    k_batch(BatchParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   typename F::S* sm = reinterpret_cast<typename F::S*>(smem_raw);
   __shared__ long long s_item;

@@ -18,8 +18,15 @@ struct BatchRange {
   int kind;
 };
 
+// Bins of 2^1..2^12 points take one range each, bins of 2^13..2^20 two.
+constexpr int kMaxBatchRanges = 32;
+
+// Passed by value, so the range table lives in the kernel's parameter space:
+// reads of it go through the constant cache and the compiler may keep them
+// in registers across the tile's barriers and stores (a table in global
+// memory has to be re-read after each of them).
 struct BatchParams {
-  const BatchRange* ranges;  // device copy, sorted by item0
+  BatchRange ranges[kMaxBatchRanges];  // sorted by item0
   int nranges;
   long long total;           // queue length
   unsigned long long* head;  // next queue item (zeroed before the launch)
@@ -27,6 +34,7 @@ struct BatchParams {
   int* err;                  // set to 1 when a bounded wait gives up (zeroed)
   unsigned int spin_limit;
 };
+static_assert(sizeof(BatchParams) <= 32000, "kernel parameters are limited to 32764 bytes");
 
 cudaError_t launch_batch(Form f, int sign, const BatchParams& P, int grid, cudaStream_t st);
 // Resident CTAs per SM; also raises the kernel's shared memory limit, so it

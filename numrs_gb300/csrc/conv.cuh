@@ -4,11 +4,13 @@
 // hardware F2F conversions between float and double run on it.  The FP32 and
 // double-float forms convert every element they read from or write to the
 // caller's f64 arrays, so those conversions are done here with integer and
-// FP32 operations on the IEEE bit patterns instead.  Values whose exponent is
-// outside the range handled below (zeros, subnormals, infinities, NaNs, and
-// magnitudes outside the normal float range) take the hardware path, which is
-// correct for every input; the bit paths are exact restatements of IEEE
-// round-to-nearest-even for the ranges they accept.
+// FP32 operations on the IEEE bit patterns instead.  d2f and f2d are integer
+// restatements of IEEE round-to-nearest-even for every input: with a hardware
+// conversion kept for the rare cases, the FP64-pipe counters still showed one
+// instruction per converted element (the rare path was evaluated on the
+// common one).  The
+// double-float split and join below keep a hardware path for values outside
+// their bit paths' ranges.
 //
 // The same source compiles for the host (g++) so that tests/test_conv.py can
 // check every path against the compiler's own conversions.
@@ -47,30 +49,93 @@ GBFFT_HD float bitsf(uint32_t b) {
   return x;
 }
 
-// double -> float, round to nearest even.  Bit path for results that are
-// normal floats: biased double exponent 897..1150 before rounding.
+GBFFT_HD uint32_t clz32(uint32_t v) {
+#if defined(__CUDA_ARCH__)
+  return (uint32_t)__clz((int)v);
+#else
+  return v ? (uint32_t)__builtin_clz(v) : 32u;
+#endif
+}
+
+// d2f for the biased exponents outside 897..1150 (infinities, NaNs,
+// overflow, subnormal and zero results); returns the float's bits without
+// the sign.  Integer operations only, so that no conversion instruction can be
+// hoisted out of the rare branch into the common path.
+GBFFT_HD uint32_t d2f_rare(uint32_t hw, uint32_t lw, uint32_t ex) {
+  if (ex == 0x7FFu) {
+    // infinity, or a NaN made quiet with its top fraction bits kept
+    const uint32_t frac = ((hw & 0xFFFFFu) << 3) | (lw >> 29);
+    return (((hw & 0xFFFFFu) | lw) != 0u) ? (0x7FC00000u | frac) : 0x7F800000u;
+  }
+  if (ex > 1150u) return 0x7F800000u;  // rounds to infinity
+  // The value is S * 2^(ex - 1075) with S = 2^52 + fraction; in units of the
+  // smallest subnormal float 2^-149 it is S / 2^(926 - ex), below one half
+  // for ex < 873 (double subnormals and zero included).
+  if (ex < 873u) return 0u;
+  const uint64_t S = ((uint64_t)((hw & 0xFFFFFu) | 0x100000u) << 32) | lw;
+  const uint32_t sh = 926u - ex;  // 30..53
+  const uint64_t q = S >> sh;
+  const uint64_t rem = S & ((1ull << sh) - 1ull);
+  const uint64_t half = 1ull << (sh - 1u);
+  const uint32_t up = (uint32_t)(rem > half) | ((uint32_t)(rem == half) & (uint32_t)(q & 1u));
+  // q + up = 2^23 is the smallest normal float, as IEEE rounding gives
+  return (uint32_t)q + up;
+}
+
+// double -> float, round to nearest even, for every input.  The common case
+// (a normal float result, biased double exponent 897..1150 before rounding)
+// is a handful of integer operations.
 GBFFT_HD float d2f(double x) {
   const uint64_t b = dbits(x);
   const uint32_t hw = (uint32_t)(b >> 32), lw = (uint32_t)b;
   const uint32_t ex = (hw >> 20) & 0x7FFu;
-  if (ex < 897u || ex > 1150u) return (float)x;
-  const uint32_t mant = ((hw & 0xFFFFFu) << 3) | (lw >> 29);  // top 23 fraction bits
-  const uint32_t rest = lw & 0x1FFFFFFFu;                       // 29 dropped bits
-  const uint32_t up = (rest > 0x10000000u) | ((rest == 0x10000000u) & (mant & 1u));
-  // a carry out of the fraction bumps the exponent, as IEEE rounding does;
-  // 1150 + carry gives 0x7F800000 (infinity), also as IEEE rounding does
-  const uint32_t r = ((ex - 896u) << 23) + mant + up;
+  uint32_t r;
+  if (ex - 897u <= 253u) {
+    const uint32_t mant = ((hw & 0xFFFFFu) << 3) | (lw >> 29);  // top 23 fraction bits
+    const uint32_t rest = lw & 0x1FFFFFFFu;                       // 29 dropped bits
+    const uint32_t up = (rest > 0x10000000u) | ((rest == 0x10000000u) & (mant & 1u));
+    // a carry out of the fraction bumps the exponent, as IEEE rounding does;
+    // 1150 + carry gives 0x7F800000 (infinity), also as IEEE rounding does
+    r = ((ex - 896u) << 23) + mant + up;
+  } else {
+    r = d2f_rare(hw, lw, ex);
+  }
   return bitsf((hw & 0x80000000u) | r);
 }
 
-// float -> double, exact.  Bit path for normal floats.
+// f2d for zeros, subnormals, infinities and NaNs (NaNs made quiet); writes
+// the double's high and low words without the sign.
+GBFFT_HD void f2d_rare(uint32_t e8, uint32_t frac, uint32_t& hw, uint32_t& lw) {
+  if (e8 == 0xFFu) {
+    hw = 0x7FF00000u | (frac >> 3) | (frac ? 0x80000u : 0u);
+    lw = frac << 29;
+    return;
+  }
+  if (frac == 0u) {
+    hw = 0u;
+    lw = 0u;
+    return;
+  }
+  // subnormal: frac * 2^-149 with its leading one at bit p
+  const uint32_t p = 31u - clz32(frac);  // 0..22
+  const uint32_t m = frac << (23u - p);  // leading one at bit 23
+  hw = ((p + 874u) << 20) | ((m & 0x7FFFFFu) >> 3);
+  lw = m << 29;
+}
+
+// float -> double, exact, for every input.
 GBFFT_HD double f2d(float x) {
   const uint32_t f = fbits(x);
   const uint32_t e8 = (f >> 23) & 0xFFu;
-  if (e8 == 0u || e8 == 0xFFu) return (double)x;
-  const uint64_t hw = (uint64_t)((f & 0x80000000u) | ((e8 + 896u) << 20) | ((f & 0x7FFFFFu) >> 3));
-  const uint64_t lw = (uint64_t)(f & 7u) << 29;
-  return bitsd((hw << 32) | lw);
+  const uint32_t frac = f & 0x7FFFFFu;
+  uint32_t hw, lw;
+  if (e8 - 1u < 254u) {
+    hw = ((e8 + 896u) << 20) | (frac >> 3);
+    lw = frac << 29;
+  } else {
+    f2d_rare(e8, frac, hw, lw);
+  }
+  return bitsd(((uint64_t)((f & 0x80000000u) | hw) << 32) | lw);
 }
 
 // Exact value of a 29-bit unsigned integer r, rounded to float (two magic-number

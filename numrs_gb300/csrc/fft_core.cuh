@@ -365,10 +365,24 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
   tile_compute_store<F, SG, OUT, T>(p, line0, j0, sm, tid);
 }
 
-// One CTA per tile.  Two 256-thread CTAs fit on an SM (registers capped at
-// 128, shared memory 2 x 70 KB), which covers the FP64 pipe's latency.
+// Resident 256-thread CTAs per SM that a pass kernel is compiled for.  The
+// FP64 and double-float forms keep two (128 registers, 2 x 70 KB of shared
+// memory), which covers the FP64 pipe's latency and holds their working set
+// without spills.  The FP32 forms are memory-latency bound, so they trade
+// registers for resident warps: four CTAs (64 registers) when the input is
+// FP32 scratch, three (80 registers) when it is the caller's f64 data, whose
+// sixteen in-flight loads per thread need twice the registers.
+template <class F, int IN>
+constexpr int pass_min_blocks() {
+  if constexpr (F::kind == 1 && !F::kTensor) return IN == IO_D2 ? 3 : 4;
+  else if constexpr (F::kind == 1) return 3;
+  else return 2;
+}
+
+// One CTA per tile.
 template <class F, int SG, int IN, int OUT, int T>
-__global__ void __launch_bounds__(T, (T == 256 ? 2 : 1)) k_pass(PassParams p) {
+__global__ void __launch_bounds__(T, (T == 256 ? pass_min_blocks<F, IN>() : 1))
+    k_pass(PassParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   pass_tile<F, SG, IN, OUT, T, false>(p, blockIdx.x, reinterpret_cast<typename F::S*>(smem_raw),
                                       threadIdx.x);

@@ -626,7 +626,7 @@ struct BatchPlan {
   std::vector<size_t> nn;
   std::vector<const void*> ptrs;
   int form = -1, sign = 0;
-  DevBuf ranges, ptrtab, done, flags, scratch;
+  DevBuf ptrtab, done, flags, scratch;
   BatchParams P;
   int grid = 0;
   bool prefetch = false;  // bulk-copy prefetching kernel
@@ -637,10 +637,10 @@ struct BatchPlan {
 BatchPlan g_batch;
 
 void batch_plan_free(BatchPlan& b) {
-  if (b.exec || b.ranges.p) cudaDeviceSynchronize();  // an earlier replay may be in flight
+  if (b.exec || b.done.p) cudaDeviceSynchronize();  // an earlier replay may be in flight
   if (b.exec) cudaGraphExecDestroy(b.exec);
   b.exec = nullptr;
-  for (DevBuf* d : {&b.ranges, &b.ptrtab, &b.done, &b.flags, &b.scratch}) {
+  for (DevBuf* d : {&b.ptrtab, &b.done, &b.flags, &b.scratch}) {
     if (d->p) cudaFree(d->p);
     d->p = nullptr;
     d->bytes = 0;
@@ -725,13 +725,13 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
     r.item0 = item;
     item += r.p.tiles;
   }
-  TRY(ensure(b.ranges, std::max<size_t>(all.size(), 1) * sizeof(BatchRange)));
-  if (!all.empty())
-    CK(cudaMemcpy(b.ranges.p, all.data(), all.size() * sizeof(BatchRange), cudaMemcpyHostToDevice));
+  if (all.size() > (size_t)kMaxBatchRanges)
+    return fail(GBFFT_UNSUPPORTED_SIZE, "batch: %zu size ranges (at most %d)", all.size(),
+                kMaxBatchRanges);
   TRY(ensure(b.done, std::max<size_t>(count, 1) * sizeof(unsigned int)));
   TRY(ensure(b.flags, 64));
   std::memset(&b.P, 0, sizeof b.P);
-  b.P.ranges = (const BatchRange*)b.ranges.p;
+  for (size_t i = 0; i < all.size(); ++i) b.P.ranges[i] = all[i];
   b.P.nranges = (int)all.size();
   b.P.total = item;
   b.P.head = (unsigned long long*)b.flags.p;
@@ -740,13 +740,15 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
   b.P.spin_limit = 1u << 24;
   int dev_sms = 0;
   CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, g.device));
-  // The prefetching kernel needs 16-byte aligned caller arrays (bulk copies);
-  // the FP64 form is FP64-pipe bound and gains nothing from it.
+  // The prefetching kernel (opt-in: GBFFT_BATCH_PREFETCH=1) needs 16-byte
+  // aligned caller arrays for its bulk copies.  Measured on the 20,000-transform
+  // batch it is slower than k_batch in every form (FP32 1.75 vs 1.37 ms): its
+  // staging buffer costs a resident CTA per SM and the copies wait at barriers.
   bool aligned = true;
   for (size_t i = 0; i < count; ++i)
     if (((uintptr_t)dptrs[i]) & 15u) aligned = false;
   const char* pfenv = getenv("GBFFT_BATCH_PREFETCH");
-  b.prefetch = f != FORM_F64 && aligned && !(pfenv && pfenv[0] == '0');
+  b.prefetch = f != FORM_F64 && aligned && pfenv && pfenv[0] == '1';
   int per = b.prefetch ? batch_pf_blocks_per_sm(f, sign) : batch_blocks_per_sm(f, sign);
   if (per < 1) per = 1;
   b.grid = (int)std::min<long long>((long long)dev_sms * per, std::max<long long>(item, 1));

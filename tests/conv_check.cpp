@@ -21,14 +21,21 @@ int main(int argc, char** argv) {
   for (long i = 0; i < n; ++i) {
     // random doubles: random bits (all exponents) and random scaled normals
     double x = (i & 1) ? bitsd(next()) : ldexp((double)(int64_t)next() / 9.2e18, (int)(next() % 300) - 150);
-    if (std::isnan(x)) continue;
+    // every other draw: a double near or below the float subnormal range
+    if ((i & 3) == 2) x = ldexp((double)(int64_t)next() / 9.2e18, -120 - (int)(next() % 40));
+    // NaNs included: both conversions make them quiet and keep the top
+    // payload bits, as the host's IEEE conversions do
     float a = d2f(x), b = (float)x;
-    if (fbits(a) != fbits(b) && !(std::isnan(a) && std::isnan(b))) {
+    if (fbits(a) != fbits(b)) {
       printf("d2f mismatch %a -> %a vs %a\n", x, a, b);
       return 1;
     }
-    float f = bitsf((uint32_t)next());
-    if (!std::isnan(f)) {
+    // random float bits, every fourth one a subnormal, zero or non-finite
+    uint32_t fb = (uint32_t)next();
+    if ((i & 3) == 1) fb &= 0x807FFFFFu;
+    if ((i & 7) == 3) fb |= 0x7F800000u;
+    float f = bitsf(fb);
+    {
       double c = f2d(f), e = (double)f;
       if (dbits(c) != dbits(e)) {
         printf("f2d mismatch %a -> %a vs %a\n", f, c, e);
@@ -56,6 +63,21 @@ int main(int argc, char** argv) {
       double d3 = df2d(p2, t), w3 = (double)p2 + (double)t;
       if (std::fabs(d3 - w3) > std::ldexp(std::fabs(w3), -51)) {
         printf("df2d corner (%a, %a) -> %a vs %a\n", p2, t, d3, w3);
+        return 1;
+      }
+    }
+  }
+  // exact corner values: zeros, infinities, the float range limits and the
+  // halfway points around them
+  const double corners[] = {0.0, -0.0, HUGE_VAL, -HUGE_VAL, 3.4028234663852886e38,
+                            3.4028235677973366e38, 3.4028235677973362e38, 1.1754943508222875e-38,
+                            1.1754942807573643e-38, 1.401298464324817e-45, 7.006492321624085e-46,
+                            7.006492321624087e-46, 2.1019476964872256e-45, 4.9406564584124654e-324};
+  for (double c : corners) {
+    for (int sgn = 0; sgn < 2; ++sgn) {
+      const double x = sgn ? -c : c;
+      if (fbits(d2f(x)) != fbits((float)x)) {
+        printf("d2f corner mismatch %a\n", x);
         return 1;
       }
     }

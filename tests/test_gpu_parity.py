@@ -120,6 +120,28 @@ def test_fft_batch_uneven(nr, form):
         check(w, ref, int(s).bit_length() - 1, form, "fft_batch nn=%d" % s)
 
 
+@pytest.mark.parametrize("form", [f for f in FORMS if f != "fp64"])
+def test_fft_batch_prefetch_kernel(nr, form, monkeypatch):
+    """The opt-in prefetching persistent kernel (bulk copies of the next tile
+    into shared memory) against the oracle, single- and two-pass bins."""
+    torch = pytest.importorskip("torch")
+    monkeypatch.setenv("GBFFT_BATCH_PREFETCH", "1")
+    sizes = [64, 8192, 128, 16384, 4096, 256, 2, 8192, 512, 32] * 4
+    data = [W.normal(700 + i, 2 * s) for i, s in enumerate(sizes)]
+    tens = [torch.from_numpy(a.copy()).cuda() for a in data]
+    b = nr.FFTBatch(tens, form=form)
+    for sg in (-1, -1):
+        for t, a in zip(tens, data):
+            t.copy_(torch.from_numpy(a))
+        b.run(sg)
+        torch.cuda.synchronize()
+        for a, t, s in zip(data, tens, sizes):
+            ref = a.copy()
+            O.four1(ref, s, sg)
+            check(t.cpu().numpy(), ref, max(1, s.bit_length() - 1), form,
+                  "prefetch batch nn=%d isign=%d" % (s, sg))
+
+
 @pytest.mark.parametrize("form", FORMS)
 def test_fft_batch_device_graph_replay(nr, form):
     """Device tensors through the persistent batched launch: the first call
