@@ -206,22 +206,7 @@ __global__ void __launch_bounds__(256, (F::kind == 2 ? 1 : 2)) k_batch_pf(BatchP
       if (!s_ok) break;  // error already recorded; the host reports GBFFT_TIMEOUT
       using IE = typename IOElem<SIO>::T;
       IE raw[kEPT];
-#pragma unroll
-      for (int k = 0; k < kEPT; ++k) {
-        bool valid;
-        const IE* src = elem_src<SIO>(p, line0, j0, tid + k * 256, valid);
-        if (valid) {
-          if constexpr (sizeof(IE) == 8) {
-            float2 t = __ldcg(reinterpret_cast<const float2*>(src));
-            memcpy(&raw[k], &t, 8);
-          } else {
-            float4 t = __ldcg(reinterpret_cast<const float4*>(src));
-            memcpy(&raw[k], &t, 16);
-          }
-        } else {
-          memset(&raw[k], 0, sizeof(IE));
-        }
-      }
+      load_tile_raw<IE, SIO, 256, true>(p, line0, j0, tid, raw);
 #pragma unroll
       for (int k = 0; k < kEPT; ++k) stage_elem<F, SG, SIO>(p, line0, j0, tid + k * 256, raw[k], sm);
     }

@@ -14,7 +14,7 @@
 
 namespace gbfft {
 
-constexpr int kEPT = 16;  // complex elements per thread per tile
+constexpr int kEPT = kTileEPT;  // complex elements per thread per tile
 
 __device__ __forceinline__ int pidx(int i, int sh) { return i + (i >> sh); }
 
@@ -23,17 +23,18 @@ __device__ __forceinline__ int pidx(int i, int sh) { return i + (i >> sh); }
 namespace gbfft {
 
 // ---------------------------------------------------------------------------
-// Twiddle lookup: w_S^e with sign, S and e < S powers-of-two arithmetic.
+// Twiddle lookup: w_S^e with sign, S = 2^logS and 0 <= e < S <= 2^29, so
+// that every index fits 32-bit arithmetic.
 // ---------------------------------------------------------------------------
 template <class F>
-__device__ __forceinline__ typename F::C twiddle(const Twiddles& tw, int logS, long long e,
+__device__ __forceinline__ typename F::C twiddle(const Twiddles& tw, int logS, unsigned int e,
                                                  int sg) {
   using TW = typename F::TW;
   const TW* dense = reinterpret_cast<const TW*>(tw.dense);
-  if (logS <= kDenseLog) return F::ld_tw(dense + ((1ll << logS) + e), sg);
+  if (logS <= kDenseLog) return F::ld_tw(dense + ((1u << logS) + e), sg);
   const TW* part = reinterpret_cast<const TW*>(tw.partial);
-  typename F::C hi = F::ld_tw(dense + ((1ll << (logS - kPartialLog)) + (e >> kPartialLog)), sg);
-  typename F::C lo = F::ld_tw(part + ((long long)(logS - kDenseLog - 1) * kPartial +
+  typename F::C hi = F::ld_tw(dense + ((1u << (logS - kPartialLog)) + (e >> kPartialLog)), sg);
+  typename F::C lo = F::ld_tw(part + ((unsigned)(logS - kDenseLog - 1) * kPartial +
                                       (e & (kPartial - 1))), sg);
   return F::mul(hi, lo);
 }
@@ -145,7 +146,7 @@ __device__ __forceinline__ void subpass(typename F::S* sm, int logR, int logNs, 
     if (logNs > 0 && jm != 0) {
 #pragma unroll
       for (int t = 1; t < Q; ++t)
-        v[i][t] = F::mul(v[i][t], twiddle<F>(tw, logNs + LQ, (long long)jm * t, SG));
+        v[i][t] = F::mul(v[i][t], twiddle<F>(tw, logNs + LQ, (unsigned)(jm * t), SG));
     }
     dftq<F, SG, Q>(v[i]);
     ob[i] = base + ((j >> logNs) << (logNs + LQ)) + jm;
@@ -256,10 +257,35 @@ __device__ __forceinline__ void stage_elem(const PassParams& p, long long line0,
   C v = (line < p.nlines) ? gload<F, IN>(&rawv, 0) : F::from_d(0.0, 0.0);
   if (p.logNs > 0) {
     const long long j = (p.mode == 0) ? j0 + c : j0;
-    const long long jm = j & (p.Ns - 1);
-    if (jm != 0 && r != 0) v = F::mul(v, twiddle<F>(p.tw, p.logNs + p.logR, jm * r, SG));
+    const unsigned jm = (unsigned)(j & (p.Ns - 1));
+    // jm * r < Ns * R <= L
+    if (jm != 0 && r != 0) v = F::mul(v, twiddle<F>(p.tw, p.logNs + p.logR, jm * (unsigned)r, SG));
   }
   sm[pidx((c << p.logR) + r, F::kPadShift)] = F::to_s(v);
+}
+
+// Global index of a line's first element.
+__device__ __forceinline__ long long line_base(const PassParams& p, long long line) {
+  return (line >> p.lq_log) * p.lstride + (line & ((1ll << p.lq_log) - 1));
+}
+
+// Linear layouts (no per-line pointer table): the global index of slot k of
+// thread tid is thread_base_in/out + in_off/out_off[k].  ct receives the
+// thread's part of the slot's column, used for the column bound of mode 1.
+__device__ __forceinline__ long long thread_base_in(const PassParams& p, long long line0,
+                                                    long long j0, int tid, long long& ct) {
+  long long c, r;
+  tile_cr(tid, p.in_rcontig, p.logR, p.logC, c, r);
+  ct = c;
+  return line_base(p, line0) + j0 * p.s + col_off_in(p, c) + r * ((p.L >> p.logR) * p.s);
+}
+__device__ __forceinline__ long long thread_base_out(const PassParams& p, long long line0,
+                                                     long long j0, int tid, long long& ct) {
+  long long c, r;
+  tile_cr(tid, p.out_rcontig, p.logR, p.logC, c, r);
+  ct = c;
+  const long long jd0 = ((j0 >> p.logNs) << (p.logNs + p.logR)) + (j0 & (p.Ns - 1));
+  return line_base(p, line0) + jd0 * p.s + col_off_out(p, c) + r * (p.Ns * p.s);
 }
 
 // The R-point DFTs of the tile's columns, then the store at the autosorted
@@ -290,6 +316,25 @@ __device__ __forceinline__ void tile_compute_store(const PassParams& p, long lon
     }
     logNsub += lq;
   }
+  if (p.out_ptrs == nullptr) {
+    // linear layout: per-thread base plus the slot offsets out_off[k]
+    long long ct;
+    OE* dst = reinterpret_cast<OE*>(p.out) + thread_base_out(p, line0, j0, tid, ct);
+    const long long rem = (p.mode == 0) ? (1ll << 62) : p.nlines - line0;
+#pragma unroll 4
+    for (int k = 0; k < kEPT; ++k) {
+      const int e = tid + k * T;
+      int c, r;
+      elem_cr(e, p.out_rcontig, logR, logC, c, r);
+      long long ck, rk;
+      tile_cr((long long)k * T, p.out_rcontig, logR, logC, ck, rk);
+      if (ct + ck >= rem) continue;
+      C v = F::from_s(sm[pidx((c << logR) + r, sh)]);
+      if (p.do_scale) v = F::scale(v, p.scale);
+      gstore<F, OUT>(dst, p.out_off[k], v);
+    }
+    return;
+  }
   const long long lqmask = (1ll << p.lq_log) - 1;
 #pragma unroll 4
   for (int k = 0; k < kEPT; ++k) {
@@ -301,15 +346,14 @@ __device__ __forceinline__ void tile_compute_store(const PassParams& p, long lon
     if (line >= p.nlines) continue;
     C v = F::from_s(sm[pidx((c << logR) + r, sh)]);
     if (p.do_scale) v = F::scale(v, p.scale);
-    OE* base = p.out_ptrs
-        ? reinterpret_cast<OE*>(p.out_ptrs[line])
-        : reinterpret_cast<OE*>(p.out) + ((line >> p.lq_log) * p.lstride + (line & lqmask));
+    OE* base = reinterpret_cast<OE*>(p.out_ptrs[line]);
     const long long jd = ((j >> p.logNs) << (p.logNs + logR)) + (j & (p.Ns - 1));
     gstore<F, OUT>(base, (jd + ((long long)r << p.logNs)) * p.s, v);
   }
 }
 
-// Address of tile element e in global memory (input side).
+// Address of tile element e in global memory, input side, for tiles whose
+// lines come from a per-line pointer table.
 template <int IN>
 __device__ __forceinline__ const typename IOElem<IN>::T* elem_src(const PassParams& p,
                                                                   long long line0, long long j0,
@@ -321,17 +365,56 @@ __device__ __forceinline__ const typename IOElem<IN>::T* elem_src(const PassPara
   if (p.mode == 0) j += c; else line += c;
   valid = line < p.nlines;
   if (!valid) return nullptr;
-  const long long lqmask = (1ll << p.lq_log) - 1;
-  const IE* base = p.in_ptrs
-      ? reinterpret_cast<const IE*>(p.in_ptrs[line])
-      : reinterpret_cast<const IE*>(p.in) + ((line >> p.lq_log) * p.lstride + (line & lqmask));
+  const IE* base = reinterpret_cast<const IE*>(p.in_ptrs[line]);
   return base + (j + ((long long)r << (p.logL - p.logR))) * p.s;
 }
 
-// One full tile from global memory.  All sixteen loads of a thread are issued
-// before any is used, so that each SM keeps enough bytes in flight to cover
-// the memory latency.  L2_ONLY loads bypass L1 (data written by other CTAs of
-// the same launch).
+template <class IE, bool L2_ONLY>
+__device__ __forceinline__ void load_elem(const IE* src, IE& dst) {
+  if constexpr (L2_ONLY) {
+    if constexpr (sizeof(IE) == 8) {
+      float2 t = __ldcg(reinterpret_cast<const float2*>(src));
+      memcpy(&dst, &t, 8);
+    } else {
+      float4 t = __ldcg(reinterpret_cast<const float4*>(src));
+      memcpy(&dst, &t, 16);
+    }
+  } else {
+    dst = *src;
+  }
+}
+
+// The sixteen raw elements of thread tid's slots (zero outside the lines).
+// All loads are issued before any is used, so that each SM keeps enough
+// bytes in flight to cover the memory latency.
+template <class IE, int IN, int T, bool L2_ONLY>
+__device__ __forceinline__ void load_tile_raw(const PassParams& p, long long line0, long long j0,
+                                              int tid, IE (&raw)[kEPT]) {
+  if (p.in_ptrs == nullptr) {
+    // linear layout: per-thread base plus the slot offsets in_off[k]
+    long long ct;
+    const IE* src = reinterpret_cast<const IE*>(p.in) + thread_base_in(p, line0, j0, tid, ct);
+    const long long rem = (p.mode == 0) ? (1ll << 62) : p.nlines - line0;
+#pragma unroll
+    for (int k = 0; k < kEPT; ++k) {
+      long long ck, rk;
+      tile_cr((long long)k * T, p.in_rcontig, p.logR, p.logC, ck, rk);
+      if (ct + ck < rem) load_elem<IE, L2_ONLY>(src + p.in_off[k], raw[k]);
+      else memset(&raw[k], 0, sizeof(IE));
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kEPT; ++k) {
+      bool valid;
+      const IE* src = elem_src<IN>(p, line0, j0, tid + k * T, valid);
+      if (valid) load_elem<IE, L2_ONLY>(src, raw[k]);
+      else memset(&raw[k], 0, sizeof(IE));
+    }
+  }
+}
+
+// One full tile from global memory.  L2_ONLY loads bypass L1 (data written by
+// other CTAs of the same launch).
 template <class F, int SG, int IN, int OUT, int T, bool L2_ONLY>
 __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
                                           typename F::S* sm, int tid) {
@@ -339,26 +422,7 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
   long long line0, j0;
   tile_origin(p, tile, line0, j0);
   IE raw[kEPT];
-#pragma unroll
-  for (int k = 0; k < kEPT; ++k) {
-    bool valid;
-    const IE* src = elem_src<IN>(p, line0, j0, tid + k * T, valid);
-    if (valid) {
-      if constexpr (L2_ONLY) {
-        if constexpr (sizeof(IE) == 8) {
-          float2 t = __ldcg(reinterpret_cast<const float2*>(src));
-          memcpy(&raw[k], &t, 8);
-        } else {
-          float4 t = __ldcg(reinterpret_cast<const float4*>(src));
-          memcpy(&raw[k], &t, 16);
-        }
-      } else {
-        raw[k] = *src;
-      }
-    } else {
-      memset(&raw[k], 0, sizeof(IE));
-    }
-  }
+  load_tile_raw<IE, IN, T, L2_ONLY>(p, line0, j0, tid, raw);
 #pragma unroll
   for (int k = 0; k < kEPT; ++k) stage_elem<F, SG, IN>(p, line0, j0, tid + k * T, raw[k], sm);
   __syncthreads();
@@ -406,7 +470,9 @@ inline cudaError_t launch_pass_one(const PassParams& p, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     attr_done = smem;
   }
-  k_pass<F, SG, IN, OUT, T><<<dim3((unsigned)p.tiles), T, smem, st>>>(p);
+  PassParams q = p;
+  set_slot_offsets(q, T);
+  k_pass<F, SG, IN, OUT, T><<<dim3((unsigned)q.tiles), T, smem, st>>>(q);
   return cudaGetLastError();
 }
 

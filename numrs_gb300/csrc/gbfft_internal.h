@@ -30,6 +30,8 @@ constexpr int kMaxLog = kDenseLog + kPartialLog;  // 2^28 points per axis
 constexpr size_t kDenseEntries = size_t(2) << kDenseLog;
 constexpr size_t kPartialEntries = size_t(kMaxLog - kDenseLog) * kPartial;
 
+constexpr int kTileEPT = 16;  // complex elements per thread per tile
+
 struct Twiddles {
   const void* dense = nullptr;
   const void* partial = nullptr;
@@ -70,7 +72,50 @@ struct PassParams {
   int do_scale;
   double scale;
   long long tiles;  // grid size
+  // Per-slot parts of the global element indices of a tile, for layouts
+  // without per-line pointer tables: slot k of thread tid holds tile element
+  // e = tid + k*T, and its index is a per-thread base plus in_off[k] (load
+  // order) or out_off[k] (store order).  Filled for the launch's thread count
+  // T by set_slot_offsets.
+  long long in_off[kTileEPT];
+  long long out_off[kTileEPT];
 };
+
+// (column, row) of tile element e: e splits at bit b = logR when the tile's
+// columns are contiguous runs of rows in memory (rcontig), at b = logC
+// otherwise.  For e = tid + k*T with T a power of two, the thread's part and
+// the slot's part of e occupy disjoint bits, so the column and row of e are
+// the sums of those of tid and of k*T.
+__host__ __device__ inline void tile_cr(long long e, int rcontig, int logR, int logC, long long& c,
+                                        long long& r) {
+  if (rcontig) { r = e & ((1ll << logR) - 1); c = e >> logR; }
+  else { c = e & ((1ll << logC) - 1); r = e >> logC; }
+}
+
+// Index offset of tile column c from column 0, input and output side.  Both
+// are linear in the bit fields of c (mode 0: columns are consecutive j of one
+// line; mode 1: consecutive lines of the line grouping), so the offset of a
+// sum of disjoint-bit columns is the sum of their offsets.
+__host__ __device__ inline long long col_off_in(const PassParams& p, long long c) {
+  if (p.mode == 0) return c * p.s;
+  return (c >> p.lq_log) * p.lstride + (c & ((1ll << p.lq_log) - 1));
+}
+__host__ __device__ inline long long col_off_out(const PassParams& p, long long c) {
+  if (p.mode == 0) return (((c >> p.logNs) << (p.logNs + p.logR)) + (c & (p.Ns - 1))) * p.s;
+  return (c >> p.lq_log) * p.lstride + (c & ((1ll << p.lq_log) - 1));
+}
+
+inline void set_slot_offsets(PassParams& p, int T) {
+  const long long rs_in = (p.L >> p.logR) * p.s;
+  const long long rs_out = p.Ns * p.s;
+  for (int k = 0; k < kTileEPT; ++k) {
+    long long c, r;
+    tile_cr((long long)k * T, p.in_rcontig, p.logR, p.logC, c, r);
+    p.in_off[k] = col_off_in(p, c) + r * rs_in;
+    tile_cr((long long)k * T, p.out_rcontig, p.logR, p.logC, c, r);
+    p.out_off[k] = col_off_out(p, c) + r * rs_out;
+  }
+}
 
 // kernel launchers (one per form, defined in fft_<form>.cu)
 cudaError_t launch_pass_f64(int sign, IOType in, IOType out, const PassParams& p, int threads,

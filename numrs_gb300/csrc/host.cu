@@ -720,6 +720,8 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
   std::vector<BatchRange> all;
   for (auto* v : {&first_pass, &single, &second_pass})
     for (auto& r : *v) all.push_back(r);
+  // the persistent kernels run full 4096-element tiles on 256 threads
+  for (auto& r : all) set_slot_offsets(r.p, 256);
   long long item = 0;
   for (auto& r : all) {
     r.item0 = item;
