@@ -16,7 +16,15 @@ namespace gbfft {
 
 constexpr int kEPT = kTileEPT;  // complex elements per thread per tile
 
+// Shared-memory tile layout: column c, row r at c*cs + pidx(r).  The row
+// padding (one element per 2^sh) spreads strided accesses within a column
+// over the banks; one extra element per column (columns of 16 rows or more)
+// does the same for accesses whose lanes step across columns.
 __device__ __forceinline__ int pidx(int i, int sh) { return i + (i >> sh); }
+__host__ __device__ __forceinline__ int col_stride(int logR, int sh) {
+  const int R = 1 << logR;
+  return R + (R >> sh) + (logR >= 4 ? 1 : 0);
+}
 
 }  // namespace gbfft
 #include "tc16.cuh"
@@ -123,8 +131,8 @@ __device__ __forceinline__ void dftq(typename F::C* v) {
 // shared memory (column c at c*R, padded).  Every thread owns 16/Q butterflies.
 // ---------------------------------------------------------------------------
 template <class F, int SG, int Q>
-__device__ __forceinline__ void subpass(typename F::S* sm, int logR, int logNs, const Twiddles& tw,
-                                        int tid, int T) {
+__device__ __forceinline__ void subpass(typename F::S* sm, int logR, int cs, int logNs,
+                                        const Twiddles& tw, int tid, int T) {
   using C = typename F::C;
   constexpr int B = kEPT / Q;
   constexpr int LQ = (Q == 2) ? 1 : (Q == 4) ? 2 : (Q == 8) ? 3 : 4;
@@ -133,15 +141,15 @@ __device__ __forceinline__ void subpass(typename F::S* sm, int logR, int logNs, 
   const int RQ = 1 << logRQ;
   const int Ns = 1 << logNs;
   C v[B][Q];
-  int ob[B];
+  int ob[B], oc[B];
 #pragma unroll
   for (int i = 0; i < B; ++i) {
     const int b = tid + i * T;
     const int c = b >> logRQ;
     const int j = b & (RQ - 1);
-    const int base = c << logR;
+    const int cb = c * cs;
 #pragma unroll
-    for (int t = 0; t < Q; ++t) v[i][t] = F::from_s(sm[pidx(base + j + t * RQ, sh)]);
+    for (int t = 0; t < Q; ++t) v[i][t] = F::from_s(sm[cb + pidx(j + t * RQ, sh)]);
     const int jm = j & (Ns - 1);
     if (logNs > 0 && jm != 0) {
 #pragma unroll
@@ -149,13 +157,14 @@ __device__ __forceinline__ void subpass(typename F::S* sm, int logR, int logNs, 
         v[i][t] = F::mul(v[i][t], twiddle<F>(tw, logNs + LQ, (unsigned)(jm * t), SG));
     }
     dftq<F, SG, Q>(v[i]);
-    ob[i] = base + ((j >> logNs) << (logNs + LQ)) + jm;
+    oc[i] = cb;
+    ob[i] = ((j >> logNs) << (logNs + LQ)) + jm;
   }
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < B; ++i) {
 #pragma unroll
-    for (int t = 0; t < Q; ++t) sm[pidx(ob[i] + t * Ns, sh)] = F::to_s(v[i][t]);
+    for (int t = 0; t < Q; ++t) sm[oc[i] + pidx(ob[i] + t * Ns, sh)] = F::to_s(v[i][t]);
   }
   __syncthreads();
 }
@@ -261,7 +270,7 @@ __device__ __forceinline__ void stage_elem(const PassParams& p, long long line0,
     // jm * r < Ns * R <= L
     if (jm != 0 && r != 0) v = F::mul(v, twiddle<F>(p.tw, p.logNs + p.logR, jm * (unsigned)r, SG));
   }
-  sm[pidx((c << p.logR) + r, F::kPadShift)] = F::to_s(v);
+  sm[c * col_stride(p.logR, F::kPadShift) + pidx(r, F::kPadShift)] = F::to_s(v);
 }
 
 // Global index of a line's first element.
@@ -297,6 +306,7 @@ __device__ __forceinline__ void tile_compute_store(const PassParams& p, long lon
   using OE = typename IOElem<OUT>::T;
   constexpr int sh = F::kPadShift;
   const int logR = p.logR, logC = p.logC;
+  const int cs = col_stride(logR, sh);
   int logNsub = 0;
   for (int k = 0; k < p.nq; ++k) {
     const int lq = p.q[k];
@@ -305,14 +315,14 @@ __device__ __forceinline__ void tile_compute_store(const PassParams& p, long lon
         if constexpr (F::kTensor) {
           Dft16Frags A;
           dft16_frags<SG>(reinterpret_cast<const f2*>(p.tw.dense), A);
-          subpass16_tc<SG>(reinterpret_cast<f2*>(sm), logR, logNsub, p.tw, A, tid);
+          subpass16_tc<SG>(reinterpret_cast<f2*>(sm), logR, cs, logNsub, p.tw, A, tid);
         } else {
-          subpass<F, SG, 16>(sm, logR, logNsub, p.tw, tid, T);
+          subpass<F, SG, 16>(sm, logR, cs, logNsub, p.tw, tid, T);
         }
         break;
-      case 3: subpass<F, SG, 8>(sm, logR, logNsub, p.tw, tid, T); break;
-      case 2: subpass<F, SG, 4>(sm, logR, logNsub, p.tw, tid, T); break;
-      default: subpass<F, SG, 2>(sm, logR, logNsub, p.tw, tid, T); break;
+      case 3: subpass<F, SG, 8>(sm, logR, cs, logNsub, p.tw, tid, T); break;
+      case 2: subpass<F, SG, 4>(sm, logR, cs, logNsub, p.tw, tid, T); break;
+      default: subpass<F, SG, 2>(sm, logR, cs, logNsub, p.tw, tid, T); break;
     }
     logNsub += lq;
   }
@@ -329,7 +339,7 @@ __device__ __forceinline__ void tile_compute_store(const PassParams& p, long lon
       long long ck, rk;
       tile_cr((long long)k * T, p.out_rcontig, logR, logC, ck, rk);
       if (ct + ck >= rem) continue;
-      C v = F::from_s(sm[pidx((c << logR) + r, sh)]);
+      C v = F::from_s(sm[c * cs + pidx(r, sh)]);
       if (p.do_scale) v = F::scale(v, p.scale);
       gstore<F, OUT>(dst, p.out_off[k], v);
     }
@@ -344,7 +354,7 @@ __device__ __forceinline__ void tile_compute_store(const PassParams& p, long lon
     long long line = line0, j = j0;
     if (p.mode == 0) j += c; else line += c;
     if (line >= p.nlines) continue;
-    C v = F::from_s(sm[pidx((c << logR) + r, sh)]);
+    C v = F::from_s(sm[c * cs + pidx(r, sh)]);
     if (p.do_scale) v = F::scale(v, p.scale);
     OE* base = reinterpret_cast<OE*>(p.out_ptrs[line]);
     const long long jd = ((j >> p.logNs) << (p.logNs + logR)) + (j & (p.Ns - 1));
@@ -454,8 +464,9 @@ __global__ void __launch_bounds__(T, (T == 256 ? pass_min_blocks<F, IN>() : 1))
 
 template <class F>
 inline size_t pass_smem_bytes(int T) {
+  // rows padded as pidx, plus one element for each column of 16 rows or more
   const int E = kEPT * T;
-  return sizeof(typename F::S) * (size_t)(E + (E >> F::kPadShift));
+  return sizeof(typename F::S) * (size_t)(E + (E >> F::kPadShift) + E / 16);
 }
 
 // Launch one k_pass instantiation; its dynamic shared memory limit is raised

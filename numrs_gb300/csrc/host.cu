@@ -331,18 +331,36 @@ int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale = 1.
   Twiddles tw;
   TRY(tables(f, tw));
   const IOType sio = scratch_io(f);
-  if (ap.scratch_elems) TRY(ensure(g.scratch, ap.scratch_elems * io_bytes(sio)));
-  for (size_t i = 0; i < ap.passes.size(); ++i) {
+  const size_t P = ap.passes.size();
+  // With FP32 scratch (half the size of the caller's f64 data) a plan of three
+  // or more passes ping-pongs between two scratch halves, so that only the
+  // first pass reads and only the last pass writes the caller's array.
+  const bool two = sio == IO_F2 && P >= 3;
+  const size_t half = ap.scratch_elems * io_bytes(sio);
+  if (ap.scratch_elems) TRY(ensure(g.scratch, half * (two ? 2 : 1)));
+  void* sbuf[2] = {g.scratch.p, two ? (void*)((char*)g.scratch.p + half) : g.scratch.p};
+  for (size_t i = 0; i < P; ++i) {
     const Pass& ps = ap.passes[i];
+    const bool first = i == 0, last = i + 1 == P;
     PassParams p = ps.p;
     p.tw = tw;
-    p.in = ps.in_user ? data : g.scratch.p;
-    p.out = ps.out_user ? data : g.scratch.p;
-    if (i + 1 == ap.passes.size() && scale != 1.0) {
+    IOType in_t, out_t;
+    if (two) {
+      p.in = first ? data : sbuf[(i - 1) & 1];
+      p.out = last ? data : sbuf[i & 1];
+      in_t = first ? IO_D2 : sio;
+      out_t = last ? IO_D2 : sio;
+    } else {
+      p.in = ps.in_user ? data : g.scratch.p;
+      p.out = ps.out_user ? data : g.scratch.p;
+      in_t = ps.in_user ? IO_D2 : sio;
+      out_t = ps.out_user ? IO_D2 : sio;
+    }
+    if (last && scale != 1.0) {
       p.do_scale = 1;
       p.scale = scale;
     }
-    TRY(launch_pass(f, sign, ps.in_user ? IO_D2 : sio, ps.out_user ? IO_D2 : sio, p, ps.threads));
+    TRY(launch_pass(f, sign, in_t, out_t, p, ps.threads));
   }
   return GBFFT_OK;
 }

@@ -81,8 +81,8 @@ __device__ __forceinline__ void mma3(float (&d)[4], const uint32_t (&ahi)[4],
 // (layout and index rules as subpass<F, SG, 16> in fft_core.cuh).  Each warp
 // takes 32 consecutive butterflies in four chunks of 8 (the mma N dimension).
 template <int SG>
-__device__ __forceinline__ void subpass16_tc(f2* sm, int logR, int logNs, const Twiddles& tw,
-                                             const Dft16Frags& A, int tid) {
+__device__ __forceinline__ void subpass16_tc(f2* sm, int logR, int cs, int logNs,
+                                             const Twiddles& tw, const Dft16Frags& A, int tid) {
   constexpr int sh = 5;  // FP32 shared-memory padding (F32::kPadShift)
   const int lane = tid & 31, warp = tid >> 5;
   const int g = lane >> 2, q = lane & 3;
@@ -92,20 +92,20 @@ __device__ __forceinline__ void subpass16_tc(f2* sm, int logR, int logNs, const 
   const f2* twd = reinterpret_cast<const f2*>(tw.dense);
   // outputs held across the barrier: 4 chunks x (k = g, g+8) x (cols 2q, 2q+1)
   float yr[4][4], yi[4][4];
-  int obase[4][2];
+  int ocol[4][2], orow[4][2];
 #pragma unroll
   for (int ch = 0; ch < 4; ++ch) {
     // this thread's inputs: butterfly g of the chunk, elements t = q + 4i
     const int b = warp * 32 + ch * 8 + g;
     const int c = b >> logRQ;
     const int j = b & (RQ - 1);
-    const int base = c << logR;
+    const int cb = c * cs;
     const int jm = j & (Ns - 1);
     float xr[4], xi[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int t = q + 4 * i;
-      f2 v = sm[pidx(base + j + t * RQ, sh)];
+      f2 v = sm[cb + pidx(j + t * RQ, sh)];
       if (logNs > 0 && jm != 0 && t != 0) {
         const f2 w = twd[(1 << (logNs + 4)) + ((jm * t) & ((Ns << 4) - 1))];
         const float wy = SG > 0 ? w.y : -w.y;
@@ -147,17 +147,18 @@ __device__ __forceinline__ void subpass16_tc(f2* sm, int logR, int logNs, const 
       const int bo = warp * 32 + ch * 8 + 2 * q + cc;
       const int co = bo >> logRQ;
       const int jo = bo & (RQ - 1);
-      obase[ch][cc] = (co << logR) + ((jo >> logNs) << (logNs + 4)) + (jo & (Ns - 1));
+      ocol[ch][cc] = co * cs;
+      orow[ch][cc] = ((jo >> logNs) << (logNs + 4)) + (jo & (Ns - 1));
     }
   }
   __syncthreads();
 #pragma unroll
   for (int ch = 0; ch < 4; ++ch) {
     // c0 (k=g, col 2q) c1 (k=g, col 2q+1) c2 (k=g+8, col 2q) c3 (k=g+8, col 2q+1)
-    sm[pidx(obase[ch][0] + g * Ns, sh)] = f2{yr[ch][0], yi[ch][0]};
-    sm[pidx(obase[ch][1] + g * Ns, sh)] = f2{yr[ch][1], yi[ch][1]};
-    sm[pidx(obase[ch][0] + (g + 8) * Ns, sh)] = f2{yr[ch][2], yi[ch][2]};
-    sm[pidx(obase[ch][1] + (g + 8) * Ns, sh)] = f2{yr[ch][3], yi[ch][3]};
+    sm[ocol[ch][0] + pidx(orow[ch][0] + g * Ns, sh)] = f2{yr[ch][0], yi[ch][0]};
+    sm[ocol[ch][1] + pidx(orow[ch][1] + g * Ns, sh)] = f2{yr[ch][1], yi[ch][1]};
+    sm[ocol[ch][0] + pidx(orow[ch][0] + (g + 8) * Ns, sh)] = f2{yr[ch][2], yi[ch][2]};
+    sm[ocol[ch][1] + pidx(orow[ch][1] + (g + 8) * Ns, sh)] = f2{yr[ch][3], yi[ch][3]};
   }
   __syncthreads();
 }
