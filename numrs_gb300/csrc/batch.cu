@@ -60,14 +60,14 @@ __global__ void __launch_bounds__(256, (F::kind == 1 && !F::kTensor ? 3 : 2))
       }
       __syncthreads();
       if (!s_ok) continue;
-      pass_tile<F, SG, SIO, IO_D2, 256, true>(p, tile, sm, tid);
+      run_tile<F, SG, SIO, IO_D2, 256, true, true>(p, tile, sm, tid);
     } else if (R.kind == 1) {
-      pass_tile<F, SG, IO_D2, SIO, 256, false>(p, tile, sm, tid);
+      run_tile<F, SG, IO_D2, SIO, 256, false, true>(p, tile, sm, tid);
       __threadfence();
       __syncthreads();
       if (tid == 0) atomicAdd(P.done + R.first + line0, 1u);
     } else {
-      pass_tile<F, SG, IO_D2, IO_D2, 256, false>(p, tile, sm, tid);
+      run_tile<F, SG, IO_D2, IO_D2, 256, false, true>(p, tile, sm, tid);
     }
     __syncthreads();
   }

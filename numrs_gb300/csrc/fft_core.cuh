@@ -240,9 +240,12 @@ __device__ __forceinline__ void tile_origin(const PassParams& p, long long tile,
     line0 = tile >> logTpl;
     j0 = (tile & ((1ll << logTpl) - 1)) << p.logC;
   } else {
-    const long long ng = (p.nlines + (1ll << p.logC) - 1) >> p.logC;
-    j0 = tile / ng;
-    line0 = (tile - j0 * ng) << p.logC;
+    // tile < p.tiles < 2^31: a 32-bit division (64-bit integer division is a
+    // long software sequence that runs partly on the FP64 pipe)
+    const unsigned ng = (unsigned)((p.nlines + (1ll << p.logC) - 1) >> p.logC);
+    const unsigned jq = (unsigned)tile / ng;
+    j0 = jq;
+    line0 = (long long)((unsigned)tile - jq * ng) << p.logC;
   }
 }
 
@@ -439,6 +442,264 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
   tile_compute_store<F, SG, OUT, T>(p, line0, j0, sm, tid);
 }
 
+// ---------------------------------------------------------------------------
+// Fused form of a tile (passes of two or more in-CTA sub-passes, CUDA-core
+// forms): the first sub-pass takes its butterfly inputs straight from global
+// memory and the last one writes its outputs straight to global memory, so
+// that the tile crosses shared memory once per inner sub-pass boundary only.
+//
+// Butterfly b of a sub-pass of radix Q covers rows j + t*R/Q (t < Q) of column
+// c.  For global accesses, consecutive lanes take consecutive rows (j fastest)
+// when the tile's columns are contiguous runs of rows in memory, and
+// consecutive columns (c fastest) otherwise, so that both loads and stores stay
+// coalesced.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void butterfly_cj(int b, int rcontig, int logRQ, int logC, int& c,
+                                             int& j) {
+  if (rcontig) { j = b & ((1 << logRQ) - 1); c = b >> logRQ; }
+  else { c = b & ((1 << logC) - 1); j = b >> logC; }
+}
+
+// Global index (elements of the IO type) of row 0 of tile column c, and the
+// index step of one row; input side.
+template <int IN>
+__device__ __forceinline__ const typename IOElem<IN>::T* col_src(const PassParams& p,
+                                                                 long long line0, long long j0,
+                                                                 int c) {
+  using IE = typename IOElem<IN>::T;
+  if (p.in_ptrs == nullptr)
+    return reinterpret_cast<const IE*>(p.in) + (line_base(p, line0) + j0 * p.s + col_off_in(p, c));
+  const long long line = (p.mode == 0) ? line0 : line0 + c;
+  const long long j = (p.mode == 0) ? j0 + c : j0;
+  return reinterpret_cast<const IE*>(p.in_ptrs[line]) + j * p.s;
+}
+
+template <int OUT>
+__device__ __forceinline__ typename IOElem<OUT>::T* col_dst(const PassParams& p, long long line0,
+                                                           long long j0, int c) {
+  using OE = typename IOElem<OUT>::T;
+  const long long jd0 = ((j0 >> p.logNs) << (p.logNs + p.logR)) + (j0 & (p.Ns - 1));
+  if (p.out_ptrs == nullptr)
+    return reinterpret_cast<OE*>(p.out) + (line_base(p, line0) + jd0 * p.s + col_off_out(p, c));
+  const long long line = (p.mode == 0) ? line0 : line0 + c;
+  const long long j = (p.mode == 0) ? j0 + c : j0;
+  const long long jd = ((j >> p.logNs) << (p.logNs + p.logR)) + (j & (p.Ns - 1));
+  return reinterpret_cast<OE*>(p.out_ptrs[line]) + jd * p.s;
+}
+
+// First sub-pass (radix Q, no intra-tile twiddles) from global memory: load
+// every input of the thread's 16/Q butterflies, apply the inter-pass
+// twiddles, transform, write the outputs into the shared tile.  The caller
+// synchronises before the next sub-pass reads the tile.
+template <class F, int SG, int IN, int Q, int T, bool L2_ONLY>
+__device__ __forceinline__ void first_subpass(const PassParams& p, long long line0, long long j0,
+                                              typename F::S* sm, int cs, int tid) {
+  using C = typename F::C;
+  using IE = typename IOElem<IN>::T;
+  constexpr int B = kEPT / Q;
+  constexpr int LQ = (Q == 2) ? 1 : (Q == 4) ? 2 : (Q == 8) ? 3 : 4;
+  constexpr int sh = F::kPadShift;
+  const int logR = p.logR;
+  const int logRQ = logR - LQ;
+  const long long rs = (p.L >> logR) * p.s;  // index step of one row
+  const long long rem = (p.mode == 0) ? (1ll << 62) : p.nlines - line0;
+  IE raw[B][Q];
+  int cc[B], jj[B];
+#pragma unroll
+  for (int i = 0; i < B; ++i) {
+    butterfly_cj(tid + i * T, p.in_rcontig, logRQ, p.logC, cc[i], jj[i]);
+    if (cc[i] < rem) {
+      const IE* src = col_src<IN>(p, line0, j0, cc[i]) + jj[i] * rs;
+      const long long step = rs << logRQ;
+#pragma unroll
+      for (int t = 0; t < Q; ++t) load_elem<IE, L2_ONLY>(src + t * step, raw[i][t]);
+    } else {
+#pragma unroll
+      for (int t = 0; t < Q; ++t) memset(&raw[i][t], 0, sizeof(IE));
+    }
+  }
+  const int logS = p.logNs + logR;
+#pragma unroll
+  for (int i = 0; i < B; ++i) {
+    const int c = cc[i], j = jj[i];
+    const long long jg = (p.mode == 0) ? j0 + c : j0;
+    const unsigned jm = (unsigned)(jg & (p.Ns - 1));
+    C v[Q];
+#pragma unroll
+    for (int t = 0; t < Q; ++t) {
+      v[t] = gload<F, IN>(&raw[i][t], 0);
+      const unsigned r = (unsigned)(j + (t << logRQ));
+      // jm * r < Ns * R <= L
+      if (p.logNs > 0 && jm != 0 && r != 0) v[t] = F::mul(v[t], twiddle<F>(p.tw, logS, jm * r, SG));
+    }
+    dftq<F, SG, Q>(v);
+    const int cb = c * cs;
+#pragma unroll
+    for (int t = 0; t < Q; ++t) sm[cb + pidx(j * Q + t, sh)] = F::to_s(v[t]);
+  }
+}
+
+// Last sub-pass (radix Q, Ns = R/Q) from the shared tile to global memory:
+// twiddle, transform, scale, store at the autosorted global positions.
+template <class F, int SG, int OUT, int Q, int T>
+__device__ __forceinline__ void last_subpass(const PassParams& p, long long line0, long long j0,
+                                             const typename F::S* sm, int cs, int tid) {
+  using C = typename F::C;
+  using OE = typename IOElem<OUT>::T;
+  constexpr int B = kEPT / Q;
+  constexpr int LQ = (Q == 2) ? 1 : (Q == 4) ? 2 : (Q == 8) ? 3 : 4;
+  constexpr int sh = F::kPadShift;
+  const int logR = p.logR;
+  const int logRQ = logR - LQ;  // = log2 of the sub-pass's Ns
+  const long long rs = p.Ns * p.s;  // index step of one output row
+  const long long rem = (p.mode == 0) ? (1ll << 62) : p.nlines - line0;
+#pragma unroll
+  for (int i = 0; i < B; ++i) {
+    int c, j;
+    butterfly_cj(tid + i * T, p.out_rcontig, logRQ, p.logC, c, j);
+    const int cb = c * cs;
+    C v[Q];
+#pragma unroll
+    for (int t = 0; t < Q; ++t) v[t] = F::from_s(sm[cb + pidx(j + (t << logRQ), sh)]);
+    if (j != 0) {
+#pragma unroll
+      for (int t = 1; t < Q; ++t) v[t] = F::mul(v[t], twiddle<F>(p.tw, logR, (unsigned)(j * t), SG));
+    }
+    dftq<F, SG, Q>(v);
+    if (c >= rem) continue;
+    OE* dst = col_dst<OUT>(p, line0, j0, c) + j * rs;
+    const long long step = rs << logRQ;
+#pragma unroll
+    for (int t = 0; t < Q; ++t) {
+      C w = v[t];
+      if (p.do_scale) w = F::scale(w, p.scale);
+      gstore<F, OUT>(dst, t * step, w);
+    }
+  }
+}
+
+// A pass of one sub-pass (R = Q <= 16, single-pass transforms, whose load and
+// store layouts agree): every thread transforms 16/Q columns from global
+// memory to global memory without touching shared memory.
+template <class F, int SG, int IN, int OUT, int Q, int T, bool L2_ONLY>
+__device__ __forceinline__ void only_subpass(const PassParams& p, long long line0, long long j0,
+                                             int tid) {
+  using C = typename F::C;
+  using IE = typename IOElem<IN>::T;
+  using OE = typename IOElem<OUT>::T;
+  constexpr int B = kEPT / Q;
+  const long long rs_in = (p.L >> p.logR) * p.s;
+  const long long rs_out = p.Ns * p.s;
+  const long long rem = (p.mode == 0) ? (1ll << 62) : p.nlines - line0;
+  IE raw[B][Q];
+  int cc[B];
+#pragma unroll
+  for (int i = 0; i < B; ++i) {
+    cc[i] = tid + i * T;  // one butterfly per column
+    if (cc[i] < rem) {
+      const IE* src = col_src<IN>(p, line0, j0, cc[i]);
+#pragma unroll
+      for (int t = 0; t < Q; ++t) load_elem<IE, L2_ONLY>(src + t * rs_in, raw[i][t]);
+    } else {
+#pragma unroll
+      for (int t = 0; t < Q; ++t) memset(&raw[i][t], 0, sizeof(IE));
+    }
+  }
+  const int logS = p.logNs + p.logR;
+#pragma unroll
+  for (int i = 0; i < B; ++i) {
+    const int c = cc[i];
+    if (c >= rem) continue;
+    const long long jg = (p.mode == 0) ? j0 + c : j0;
+    const unsigned jm = (unsigned)(jg & (p.Ns - 1));
+    C v[Q];
+#pragma unroll
+    for (int t = 0; t < Q; ++t) {
+      v[t] = gload<F, IN>(&raw[i][t], 0);
+      if (p.logNs > 0 && jm != 0 && t != 0) v[t] = F::mul(v[t], twiddle<F>(p.tw, logS, jm * t, SG));
+    }
+    dftq<F, SG, Q>(v);
+    OE* dst = col_dst<OUT>(p, line0, j0, c);
+#pragma unroll
+    for (int t = 0; t < Q; ++t) {
+      C w = v[t];
+      if (p.do_scale) w = F::scale(w, p.scale);
+      gstore<F, OUT>(dst, t * rs_out, w);
+    }
+  }
+}
+
+template <class F, int SG, int IN, int T, bool L2_ONLY>
+__device__ __forceinline__ void first_subpass_q(int lq, const PassParams& p, long long line0,
+                                                long long j0, typename F::S* sm, int cs, int tid) {
+  switch (lq) {
+    case 4: first_subpass<F, SG, IN, 16, T, L2_ONLY>(p, line0, j0, sm, cs, tid); break;
+    case 3: first_subpass<F, SG, IN, 8, T, L2_ONLY>(p, line0, j0, sm, cs, tid); break;
+    case 2: first_subpass<F, SG, IN, 4, T, L2_ONLY>(p, line0, j0, sm, cs, tid); break;
+    default: first_subpass<F, SG, IN, 2, T, L2_ONLY>(p, line0, j0, sm, cs, tid); break;
+  }
+}
+
+template <class F, int SG, int OUT, int T>
+__device__ __forceinline__ void last_subpass_q(int lq, const PassParams& p, long long line0,
+                                               long long j0, const typename F::S* sm, int cs,
+                                               int tid) {
+  switch (lq) {
+    case 4: last_subpass<F, SG, OUT, 16, T>(p, line0, j0, sm, cs, tid); break;
+    case 3: last_subpass<F, SG, OUT, 8, T>(p, line0, j0, sm, cs, tid); break;
+    case 2: last_subpass<F, SG, OUT, 4, T>(p, line0, j0, sm, cs, tid); break;
+    default: last_subpass<F, SG, OUT, 2, T>(p, line0, j0, sm, cs, tid); break;
+  }
+}
+
+template <class F, int SG, int IN, int OUT, int T, bool L2_ONLY>
+__device__ __forceinline__ void pass_tile_fused(const PassParams& p, long long tile,
+                                                typename F::S* sm, int tid) {
+  long long line0, j0;
+  tile_origin(p, tile, line0, j0);
+  if (p.nq == 1) {
+    switch (p.q[0]) {
+      case 4: only_subpass<F, SG, IN, OUT, 16, T, L2_ONLY>(p, line0, j0, tid); break;
+      case 3: only_subpass<F, SG, IN, OUT, 8, T, L2_ONLY>(p, line0, j0, tid); break;
+      case 2: only_subpass<F, SG, IN, OUT, 4, T, L2_ONLY>(p, line0, j0, tid); break;
+      default: only_subpass<F, SG, IN, OUT, 2, T, L2_ONLY>(p, line0, j0, tid); break;
+    }
+    return;
+  }
+  const int cs = col_stride(p.logR, F::kPadShift);
+  first_subpass_q<F, SG, IN, T, L2_ONLY>(p.q[0], p, line0, j0, sm, cs, tid);
+  __syncthreads();
+  int logNsub = p.q[0];
+  for (int k = 1; k + 1 < p.nq; ++k) {
+    switch (p.q[k]) {
+      case 4: subpass<F, SG, 16>(sm, p.logR, cs, logNsub, p.tw, tid, T); break;
+      case 3: subpass<F, SG, 8>(sm, p.logR, cs, logNsub, p.tw, tid, T); break;
+      case 2: subpass<F, SG, 4>(sm, p.logR, cs, logNsub, p.tw, tid, T); break;
+      default: subpass<F, SG, 2>(sm, p.logR, cs, logNsub, p.tw, tid, T); break;
+    }
+    logNsub += p.q[k];
+  }
+  last_subpass_q<F, SG, OUT, T>(p.q[p.nq - 1], p, line0, j0, sm, cs, tid);
+}
+
+// One tile, fused (FUSE) or staged.  The tensor-core form always stages: its
+// radix-16 sub-passes read and write shared memory in the mma fragment layout.
+template <class F, int SG, int IN, int OUT, int T, bool L2_ONLY, bool FUSE>
+__device__ __forceinline__ void run_tile(const PassParams& p, long long tile, typename F::S* sm,
+                                         int tid) {
+  if constexpr (FUSE && !F::kTensor) pass_tile_fused<F, SG, IN, OUT, T, L2_ONLY>(p, tile, sm, tid);
+  else pass_tile<F, SG, IN, OUT, T, L2_ONLY>(p, tile, sm, tid);
+}
+
+// Whether the per-pass kernel fuses its first and last sub-passes with the
+// global loads and stores.  Measured on four1 N=2^24: FP32 passes run 13 %
+// faster fused, while the FP64-pipe bound FP64 and double-float passes run
+// 11-14 % slower (their FP64-pipe time per pass grows), so those stay staged.
+template <class F>
+constexpr bool pass_fused() {
+  return F::kind == 1 && !F::kTensor;
+}
+
 // Resident 256-thread CTAs per SM that a pass kernel is compiled for.  The
 // FP64 and double-float forms keep two (128 registers, 2 x 70 KB of shared
 // memory), which covers the FP64 pipe's latency and holds their working set
@@ -458,8 +719,8 @@ template <class F, int SG, int IN, int OUT, int T>
 __global__ void __launch_bounds__(T, (T == 256 ? pass_min_blocks<F, IN>() : 1))
     k_pass(PassParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  pass_tile<F, SG, IN, OUT, T, false>(p, blockIdx.x, reinterpret_cast<typename F::S*>(smem_raw),
-                                      threadIdx.x);
+  run_tile<F, SG, IN, OUT, T, false, pass_fused<F>()>(
+      p, blockIdx.x, reinterpret_cast<typename F::S*>(smem_raw), threadIdx.x);
 }
 
 template <class F>
@@ -481,6 +742,7 @@ inline cudaError_t launch_pass_one(const PassParams& p, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     attr_done = smem;
   }
+  if (p.tiles <= 0 || p.tiles > 0x7FFFFFFFll) return cudaErrorInvalidValue;  // grid.x limit
   PassParams q = p;
   set_slot_offsets(q, T);
   k_pass<F, SG, IN, OUT, T><<<dim3((unsigned)q.tiles), T, smem, st>>>(q);

@@ -745,6 +745,8 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
     r.item0 = item;
     item += r.p.tiles;
   }
+  if (item > 0x7FFFFFFFll)
+    return fail(GBFFT_UNSUPPORTED_SIZE, "batch: %lld tiles (at most 2^31 - 1)", item);
   if (all.size() > (size_t)kMaxBatchRanges)
     return fail(GBFFT_UNSUPPORTED_SIZE, "batch: %zu size ranges (at most %d)", all.size(),
                 kMaxBatchRanges);
