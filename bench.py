@@ -40,6 +40,24 @@ sys.path.insert(0, ROOT)
 METRIC = "FFT GFLOP/s (5N·log2N) & HBM GB/s vs peak; TC-split vs FP64 at rel-L2≤1e-6"
 FP64_PEAK_TFLOPS = 1.20  # DFMA loop measured on this machine's GB300 (probe recorded in the design doc)
 
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
+# capture of the same workload (dram__bytes_read.sum + dram__bytes_write.sum),
+# keyed by (workload, form).  The summaries under profiles/ give the commands.
+MEASURED_TRAFFIC = {
+    # 40 k_pass launches of the device-resident steps: forward 16.93 MB, inverse 8.54 MB
+    ("convlv", "fp64"): (12.74e6, "profiles/k_pass_f64_convlv_correl_n2p20.md"),
+    # the three passes of one 2^24-point transform: 367.1, 218.5, 346.0 MB
+    ("four1_24", "fp32"): (310.5e6, "profiles/k_pass_fp32_fused_four1_n2p24.md"),
+    # one persistent launch over the 20,000 transforms
+    ("batch", "fp32"): (3.2058e9, "profiles/k_batch_c3_20000_transforms.md"),
+    ("batch", "tc32"): (3.2069e9, "profiles/k_batch_c3_20000_transforms.md"),
+}
+
+
+def traffic_of(workload, form):
+    t = MEASURED_TRAFFIC.get((workload, form))
+    return (t[0], t[1]) if t else (None, None)
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -362,7 +380,8 @@ def run_convlv(args, world, rank, local):
                 "h2d_bytes_per_step": 4 * CONV_N * 8, "d2h_bytes_per_step": 2 * CONV_N * 8,
                 "host_buffers": "pinned"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None,
+                     "frac": achieved / hbm, "traffic": traffic_of("convlv", form)[0],
+                     "traffic_source": traffic_of("convlv", form)[1],
                      "kernel": "k_pass (Stockham pass)",
                      "peak_source": "%s MEASURED_PEAKS.json hbm_gbs" % hbm_kind if hbm_kind == "measured"
                      else "fallback 6.8 TB/s",
@@ -448,8 +467,9 @@ def run_four1(args, world, rank, local):
                                % (log2n, (16 * nn) >> 20), "form": args.form,
                    "l2": "input larger than L2" if nn * 16 >= (256 << 20) else "flushed between steps"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "kernel": "k_pass (Stockham pass)",
-                     "launches": pass_n, "avg_launch_ms": pass_ms / max(pass_n, 1),
+                     "frac": achieved / hbm, "traffic": traffic_of("four1_%d" % log2n, args.form)[0],
+                     "traffic_source": traffic_of("four1_%d" % log2n, args.form)[1],
+                     "kernel": "k_pass (Stockham pass)", "launches": pass_n, "avg_launch_ms": pass_ms / max(pass_n, 1),
                      "bytes_per_launch": pass_bytes / max(pass_n, 1)},
         "compute_roofline": {"bound": "fp64" if args.form == "fp64" else "fp32",
                              "achieved_tflops": pass_flops / (pass_ms / 1e3) / 1e12 if pass_ms else 0.0,
@@ -552,7 +572,8 @@ def run_batch(args, world, rank, local):
                 "h2d_bytes_per_step": total * 8, "d2h_bytes_per_step": total * 8,
                 "host_buffers": "pageable numpy arrays, packed into one staging copy"},
         "roofline": {"bound": "hbm", "achieved": main_r["hbm_gbs"], "peak": hbm, "unit": "GB/s",
-                     "frac": main_r["hbm_gbs"] / hbm, "traffic": None,
+                     "frac": main_r["hbm_gbs"] / hbm, "traffic": traffic_of("batch", args.form)[0],
+                     "traffic_source": traffic_of("batch", args.form)[1],
                      "kernel": "k_batch (persistent)"},
         "forms": results, "clocks": main_r["clocks"], "gpu_launches": main_r["launches"],
     }
