@@ -652,6 +652,190 @@ __device__ __forceinline__ void last_subpass_q(int lq, const PassParams& p, long
   }
 }
 
+// ---------------------------------------------------------------------------
+// Fused radix-16 sub-passes on the tensor cores (TC32 form).  Fragment layout,
+// splitting and products as subpass16_tc (tc16.cuh): a warp takes 32
+// butterflies in four chunks of 8; lane (g, q) holds inputs t = q + 4i of
+// butterfly g of a chunk and, after the products, outputs k = g and g + 8 of
+// butterflies 2q and 2q + 1.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void dft16_tc_products(const Dft16Frags& A, const float (&xr)[4],
+                                                  const float (&xi)[4], float (&dr)[4],
+                                                  float (&di)[4]) {
+  uint32_t rh[4], rl[4], ih[4], il[4], nh[4], nl[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    split_tf32(xr[i], rh[i], rl[i]);
+    split_tf32(xi[i], ih[i], il[i]);
+    split_tf32(-xi[i], nh[i], nl[i]);
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    dr[r] = 0.f;
+    di[r] = 0.f;
+  }
+  // Yr = Fr Xr + Fi (-Xi);  Yi = Fi Xr + Fr Xi
+  mma3(dr, A.fr_hi[0], A.fr_lo[0], rh[0], rh[1], rl[0], rl[1]);
+  mma3(dr, A.fr_hi[1], A.fr_lo[1], rh[2], rh[3], rl[2], rl[3]);
+  mma3(dr, A.fi_hi[0], A.fi_lo[0], nh[0], nh[1], nl[0], nl[1]);
+  mma3(dr, A.fi_hi[1], A.fi_lo[1], nh[2], nh[3], nl[2], nl[3]);
+  mma3(di, A.fi_hi[0], A.fi_lo[0], rh[0], rh[1], rl[0], rl[1]);
+  mma3(di, A.fi_hi[1], A.fi_lo[1], rh[2], rh[3], rl[2], rl[3]);
+  mma3(di, A.fr_hi[0], A.fr_lo[0], ih[0], ih[1], il[0], il[1]);
+  mma3(di, A.fr_hi[1], A.fr_lo[1], ih[2], ih[3], il[2], il[3]);
+}
+
+// First radix-16 sub-pass from global memory (inter-pass twiddles applied on
+// the way in) to the shared tile.
+template <int SG, int IN, bool L2_ONLY>
+__device__ __forceinline__ void first_subpass16_tc(const PassParams& p, long long line0,
+                                                   long long j0, f2* sm, int cs,
+                                                   const Dft16Frags& A, int tid) {
+  using IE = typename IOElem<IN>::T;
+  constexpr int sh = F32::kPadShift;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, q = lane & 3;
+  const int logR = p.logR, logRQ = logR - 4;
+  const long long rs = (p.L >> logR) * p.s;
+  const long long step = rs << logRQ;
+  const long long rem = (p.mode == 0) ? (1ll << 62) : p.nlines - line0;
+  const int logS = p.logNs + logR;
+  IE raw[4][4];
+  int cc[4], jj[4];
+#pragma unroll
+  for (int ch = 0; ch < 4; ++ch) {
+    butterfly_cj(warp * 32 + ch * 8 + g, p.in_rcontig, logRQ, p.logC, cc[ch], jj[ch]);
+    if (cc[ch] < rem) {
+      const IE* src = col_src<IN>(p, line0, j0, cc[ch]) + jj[ch] * rs;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) load_elem<IE, L2_ONLY>(src + (q + 4 * i) * step, raw[ch][i]);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) memset(&raw[ch][i], 0, sizeof(IE));
+    }
+  }
+#pragma unroll
+  for (int ch = 0; ch < 4; ++ch) {
+    const long long jg = (p.mode == 0) ? j0 + cc[ch] : j0;
+    const unsigned jm = (unsigned)(jg & (p.Ns - 1));
+    float xr[4], xi[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      F32::C v = gload<F32, IN>(&raw[ch][i], 0);
+      const unsigned r = (unsigned)(jj[ch] + ((q + 4 * i) << logRQ));
+      // jm * r < Ns * R <= L
+      if (p.logNs > 0 && jm != 0 && r != 0) v = F32::mul(v, twiddle<F32>(p.tw, logS, jm * r, SG));
+      xr[i] = v.x;
+      xi[i] = v.y;
+    }
+    float dr[4], di[4];
+    dft16_tc_products(A, xr, xi, dr, di);
+    // outputs k = g, g + 8 of butterflies 2q, 2q + 1 at rows 16 j + k (Ns = 1)
+#pragma unroll
+    for (int c2 = 0; c2 < 2; ++c2) {
+      int co, jo;
+      butterfly_cj(warp * 32 + ch * 8 + 2 * q + c2, p.in_rcontig, logRQ, p.logC, co, jo);
+      const int cb = co * cs;
+      sm[cb + pidx(jo * 16 + g, sh)] = f2{dr[c2], di[c2]};
+      sm[cb + pidx(jo * 16 + g + 8, sh)] = f2{dr[2 + c2], di[2 + c2]};
+    }
+  }
+}
+
+// Last radix-16 sub-pass (Ns = R/16) from the shared tile to global memory.
+template <int SG, int OUT>
+__device__ __forceinline__ void last_subpass16_tc(const PassParams& p, long long line0,
+                                                  long long j0, const f2* sm, int cs,
+                                                  const Dft16Frags& A, int tid) {
+  using OE = typename IOElem<OUT>::T;
+  constexpr int sh = F32::kPadShift;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, q = lane & 3;
+  const int logR = p.logR, logRQ = logR - 4;
+  const f2* twd = reinterpret_cast<const f2*>(p.tw.dense);
+  const long long rs = p.Ns * p.s;
+  const long long step = rs << logRQ;
+  const long long rem = (p.mode == 0) ? (1ll << 62) : p.nlines - line0;
+#pragma unroll
+  for (int ch = 0; ch < 4; ++ch) {
+    int c, j;
+    butterfly_cj(warp * 32 + ch * 8 + g, p.out_rcontig, logRQ, p.logC, c, j);
+    const int cb = c * cs;
+    float xr[4], xi[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int t = q + 4 * i;
+      f2 v = sm[cb + pidx(j + (t << logRQ), sh)];
+      if (j != 0 && t != 0) {
+        // w_R^(j t), j < R/16
+        const f2 w = twd[(1 << logR) + ((j * t) & ((1 << logR) - 1))];
+        const float wy = SG > 0 ? w.y : -w.y;
+        const float re = fmaf(v.x, w.x, -v.y * wy);
+        const float im = fmaf(v.x, wy, v.y * w.x);
+        v.x = re;
+        v.y = im;
+      }
+      xr[i] = v.x;
+      xi[i] = v.y;
+    }
+    float dr[4], di[4];
+    dft16_tc_products(A, xr, xi, dr, di);
+    // outputs k = g, g + 8 of butterflies 2q, 2q + 1 at rows j + k R/16
+#pragma unroll
+    for (int c2 = 0; c2 < 2; ++c2) {
+      int co, jo;
+      butterfly_cj(warp * 32 + ch * 8 + 2 * q + c2, p.out_rcontig, logRQ, p.logC, co, jo);
+      if (co >= rem) continue;
+      OE* dst = col_dst<OUT>(p, line0, j0, co) + jo * rs;
+      F32::C y0 = {dr[c2], di[c2]}, y1 = {dr[2 + c2], di[2 + c2]};
+      if (p.do_scale) {
+        y0 = F32::scale(y0, p.scale);
+        y1 = F32::scale(y1, p.scale);
+      }
+      gstore<F32, OUT>(dst, g * step, y0);
+      gstore<F32, OUT>(dst, (g + 8) * step, y1);
+    }
+  }
+}
+
+// Fused tile of the TC32 form: radix-16 first and last sub-passes on the
+// tensor cores straight from and to global memory; other radices on the CUDA
+// cores (the form's arithmetic is FP32).
+template <int SG, int IN, int OUT, int T, bool L2_ONLY>
+__device__ __forceinline__ void pass_tile_fused_tc(const PassParams& p, long long tile, f2* sm,
+                                                   int tid) {
+  long long line0, j0;
+  tile_origin(p, tile, line0, j0);
+  if (p.nq == 1) {
+    switch (p.q[0]) {
+      case 4: only_subpass<TC32, SG, IN, OUT, 16, T, L2_ONLY>(p, line0, j0, tid); break;
+      case 3: only_subpass<TC32, SG, IN, OUT, 8, T, L2_ONLY>(p, line0, j0, tid); break;
+      case 2: only_subpass<TC32, SG, IN, OUT, 4, T, L2_ONLY>(p, line0, j0, tid); break;
+      default: only_subpass<TC32, SG, IN, OUT, 2, T, L2_ONLY>(p, line0, j0, tid); break;
+    }
+    return;
+  }
+  const int cs = col_stride(p.logR, F32::kPadShift);
+  Dft16Frags A;
+  dft16_frags<SG>(reinterpret_cast<const f2*>(p.tw.dense), A);
+  if (p.q[0] == 4) first_subpass16_tc<SG, IN, L2_ONLY>(p, line0, j0, sm, cs, A, tid);
+  else first_subpass_q<TC32, SG, IN, T, L2_ONLY>(p.q[0], p, line0, j0, sm, cs, tid);
+  __syncthreads();
+  int logNsub = p.q[0];
+  for (int k = 1; k + 1 < p.nq; ++k) {
+    switch (p.q[k]) {
+      case 4: subpass16_tc<SG>(sm, p.logR, cs, logNsub, p.tw, A, tid); break;
+      case 3: subpass<TC32, SG, 8>(sm, p.logR, cs, logNsub, p.tw, tid, T); break;
+      case 2: subpass<TC32, SG, 4>(sm, p.logR, cs, logNsub, p.tw, tid, T); break;
+      default: subpass<TC32, SG, 2>(sm, p.logR, cs, logNsub, p.tw, tid, T); break;
+    }
+    logNsub += p.q[k];
+  }
+  const int lq = p.q[p.nq - 1];
+  if (lq == 4) last_subpass16_tc<SG, OUT>(p, line0, j0, sm, cs, A, tid);
+  else last_subpass_q<TC32, SG, OUT, T>(lq, p, line0, j0, sm, cs, tid);
+}
+
 template <class F, int SG, int IN, int OUT, int T, bool L2_ONLY>
 __device__ __forceinline__ void pass_tile_fused(const PassParams& p, long long tile,
                                                 typename F::S* sm, int tid) {
@@ -682,13 +866,17 @@ __device__ __forceinline__ void pass_tile_fused(const PassParams& p, long long t
   last_subpass_q<F, SG, OUT, T>(p.q[p.nq - 1], p, line0, j0, sm, cs, tid);
 }
 
-// One tile, fused (FUSE) or staged.  The tensor-core form always stages: its
-// radix-16 sub-passes read and write shared memory in the mma fragment layout.
+// One tile, fused (FUSE) or staged.
 template <class F, int SG, int IN, int OUT, int T, bool L2_ONLY, bool FUSE>
 __device__ __forceinline__ void run_tile(const PassParams& p, long long tile, typename F::S* sm,
                                          int tid) {
-  if constexpr (FUSE && !F::kTensor) pass_tile_fused<F, SG, IN, OUT, T, L2_ONLY>(p, tile, sm, tid);
-  else pass_tile<F, SG, IN, OUT, T, L2_ONLY>(p, tile, sm, tid);
+  if constexpr (FUSE && !F::kTensor) {
+    pass_tile_fused<F, SG, IN, OUT, T, L2_ONLY>(p, tile, sm, tid);
+  } else if constexpr (FUSE) {
+    pass_tile_fused_tc<SG, IN, OUT, T, L2_ONLY>(p, tile, reinterpret_cast<f2*>(sm), tid);
+  } else {
+    pass_tile<F, SG, IN, OUT, T, L2_ONLY>(p, tile, sm, tid);
+  }
 }
 
 // Whether the per-pass kernel fuses its first and last sub-passes with the
@@ -697,21 +885,21 @@ __device__ __forceinline__ void run_tile(const PassParams& p, long long tile, ty
 // 11-14 % slower (their FP64-pipe time per pass grows), so those stay staged.
 template <class F>
 constexpr bool pass_fused() {
-  return F::kind == 1 && !F::kTensor;
+  return F::kind == 1;
 }
 
 // Resident 256-thread CTAs per SM that a pass kernel is compiled for.  The
-// FP64 and double-float forms keep two (128 registers, 2 x 70 KB of shared
+// FP64 and double-float forms keep two (128 registers, 2 x 74 KB of shared
 // memory), which covers the FP64 pipe's latency and holds their working set
-// without spills.  The FP32 forms are memory-latency bound, so they trade
+// without spills.  The FP32 form is memory-latency bound, so it trades
 // registers for resident warps: four CTAs (64 registers) when the input is
 // FP32 scratch, three (80 registers) when it is the caller's f64 data, whose
-// sixteen in-flight loads per thread need twice the registers.
+// sixteen in-flight loads per thread need twice the registers.  TC32 keeps two:
+// its DFT-matrix fragments alone take 32 registers.
 template <class F, int IN>
 constexpr int pass_min_blocks() {
   if constexpr (F::kind == 1 && !F::kTensor) return IN == IO_D2 ? 3 : 4;
-  else if constexpr (F::kind == 1) return 3;
-  else return 2;
+  else return 2;  // FP64, double-float, and TC32 (its fragments need the registers)
 }
 
 // One CTA per tile.
