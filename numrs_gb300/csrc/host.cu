@@ -569,6 +569,22 @@ int check_isign(int isign) {
   return GBFFT_OK;
 }
 
+// The kernels move complex values as 16-byte vectors, so every array they
+// touch in place must start on a 16-byte boundary.  Host arrays are staged
+// through aligned device buffers when they are not (the direct host path is
+// taken only for aligned arrays); device arrays must be aligned by the caller
+// (cudaMalloc and torch allocations always are), and an unaligned one is
+// rejected before any launch.
+inline bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+int dev_aligned(const Call& c, const char* fn, std::initializer_list<const void*> ptrs) {
+  if (!c.dev()) return GBFFT_OK;
+  for (const void* q : ptrs)
+    if (q && !al16(q))
+      return fail(GBFFT_INVALID_ARG, "%s: device arrays must start on a 16-byte boundary", fn);
+  return GBFFT_OK;
+}
+
 // ---------------------------------------------------------------------------
 // realft on device data (n reals, power of two >= 2), `batch` lines `dist`
 // doubles apart.
@@ -648,6 +664,7 @@ struct BatchPlan {
   BatchParams P;
   int grid = 0;
   bool prefetch = false;  // bulk-copy prefetching kernel
+  bool host = false;      // the arrays are host memory, accessed directly
   cudaGraphExec_t exec = nullptr;
   long long launches_per_call = 0;
   bool valid = false;
@@ -667,12 +684,13 @@ void batch_plan_free(BatchPlan& b) {
 }
 
 int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const size_t* nn,
-                     size_t count) {
+                     size_t count, bool host_ptrs) {
   batch_plan_free(b);
   b.nn.assign(nn, nn + count);
   b.ptrs.assign((const void* const*)dptrs, (const void* const*)dptrs + count);
   b.form = f;
   b.sign = sign;
+  b.host = host_ptrs;
   std::vector<size_t> order(count);
   for (size_t i = 0; i < count; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t c) { return nn[a] > nn[c]; });
@@ -770,7 +788,8 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
   for (size_t i = 0; i < count; ++i)
     if (((uintptr_t)dptrs[i]) & 15u) aligned = false;
   const char* pfenv = getenv("GBFFT_BATCH_PREFETCH");
-  b.prefetch = f != FORM_F64 && aligned && pfenv && pfenv[0] == '1';
+  // (bulk copies are not used on host memory)
+  b.prefetch = f != FORM_F64 && aligned && !host_ptrs && pfenv && pfenv[0] == '1';
   int per = b.prefetch ? batch_pf_blocks_per_sm(f, sign) : batch_blocks_per_sm(f, sign);
   if (per < 1) per = 1;
   b.grid = (int)std::min<long long>((long long)dev_sms * per, std::max<long long>(item, 1));
@@ -797,8 +816,10 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
 }
 
 bool batch_plan_matches(const BatchPlan& b, Form f, int sign, double* const* dptrs,
-                        const size_t* nn, size_t count) {
-  if (!b.valid || b.form != (int)f || b.sign != sign || b.nn.size() != count) return false;
+                        const size_t* nn, size_t count, bool host_ptrs) {
+  if (!b.valid || b.form != (int)f || b.sign != sign || b.nn.size() != count ||
+      b.host != host_ptrs)
+    return false;
   for (size_t i = 0; i < count; ++i)
     if (b.nn[i] != nn[i] || b.ptrs[i] != (const void*)dptrs[i]) return false;
   return true;
@@ -807,7 +828,7 @@ bool batch_plan_matches(const BatchPlan& b, Form f, int sign, double* const* dpt
 // Transforms of at most 2^20 points go through the persistent launch; larger
 // ones (rare in a batch) run their own pass schedule.
 int run_batch_dev(Form f, int sign, double* const* dptrs, const size_t* nn, size_t count,
-                  bool check_err) {
+                  bool check_err, bool host_ptrs = false) {
   std::vector<double*> small_p, big_p;
   std::vector<size_t> small_n, big_n;
   for (size_t i = 0; i < count; ++i) {
@@ -815,8 +836,10 @@ int run_batch_dev(Form f, int sign, double* const* dptrs, const size_t* nn, size
     else { big_p.push_back(dptrs[i]); big_n.push_back(nn[i]); }
   }
   if (!small_p.empty()) {
-    if (!batch_plan_matches(g_batch, f, sign, small_p.data(), small_n.data(), small_p.size()))
-      TRY(build_batch_plan(g_batch, f, sign, small_p.data(), small_n.data(), small_p.size()));
+    if (!batch_plan_matches(g_batch, f, sign, small_p.data(), small_n.data(), small_p.size(),
+                            host_ptrs))
+      TRY(build_batch_plan(g_batch, f, sign, small_p.data(), small_n.data(), small_p.size(),
+                           host_ptrs));
     {
       ProfScope ps(PK_PASS, 0.0);
       CK(cudaGraphLaunch(g_batch.exec, g.cur));
@@ -971,12 +994,13 @@ int gbfft_four1(double* data, size_t nn, int isign, const gbfft_opts* opts) {
   Call c(opts);
   TRY(check_form(c));
   if (!data) return fail(GBFFT_INVALID_ARG, "four1: null data");
+  TRY(dev_aligned(c, "four1", {data}));
   TRY(check_isign(isign));
   if (!is_pow2(nn) || ilog2(nn) > kMaxAxisLog)
     return fail(GBFFT_UNSUPPORTED_SIZE, "four1: nn=%zu must be a power of two <= 2^%d", nn, kMaxAxisLog);
   TRY(init_locked(g.device));
   StreamScope ss(c);
-  if (!c.dev() && nn > 1 && direct_fits((long long)nn, 1, c.form())) {
+  if (!c.dev() && nn > 1 && al16(data) && direct_fits((long long)nn, 1, c.form())) {
     // the first pass reads the caller's array, the last pass writes it back
     TRY(run_axis_io(c.form(), isign, axis_plan((long long)nn, 1, 1, 0, (long long)nn, c.form()), data,
                     nullptr, data));
@@ -995,6 +1019,7 @@ int gbfft_four1_many(double* data, size_t nn, size_t count, size_t dist, int isi
   Call c(opts);
   TRY(check_form(c));
   if (!data && count) return fail(GBFFT_INVALID_ARG, "four1_many: null data");
+  TRY(dev_aligned(c, "four1_many", {data}));
   TRY(check_isign(isign));
   if (!is_pow2(nn) || ilog2(nn) > kMaxAxisLog)
     return fail(GBFFT_UNSUPPORTED_SIZE, "four1_many: nn=%zu must be a power of two", nn);
@@ -1020,6 +1045,7 @@ int gbfft_four1_batch(double* const* ptrs, const size_t* nn, size_t count, int i
   if (!ptrs || !nn) return fail(GBFFT_INVALID_ARG, "four1_batch: null arrays");
   for (size_t t = 0; t < count; ++t) {
     if (!ptrs[t]) return fail(GBFFT_INVALID_ARG, "four1_batch: null pointer at %zu", t);
+    TRY(dev_aligned(c, "four1_batch", {ptrs[t]}));
     if (!is_pow2(nn[t]) || ilog2(nn[t]) > kMaxAxisLog)
       return fail(GBFFT_UNSUPPORTED_SIZE, "four1_batch: nn[%zu]=%zu", t, nn[t]);
   }
@@ -1030,7 +1056,17 @@ int gbfft_four1_batch(double* const* ptrs, const size_t* nn, size_t count, int i
     TRY(run_batch_dev(c.form(), isign, ptrs, nn, count, check));
     return ss.finish(c);
   }
-  // host arrays: pack into one staging buffer (one copy each way)
+  // Host arrays.  When the GPU reaches pageable host memory directly and every
+  // array is 16-byte aligned (and fits the persistent launch), the batched
+  // kernel reads and writes the caller's arrays in place: no staging copies.
+  bool direct = g.host_direct;
+  for (size_t t = 0; direct && t < count; ++t)
+    if (!al16(ptrs[t]) || ilog2(nn[t]) > kBatchMaxLog) direct = false;
+  if (direct) {
+    TRY(run_batch_dev(c.form(), isign, ptrs, nn, count, true, true));
+    return ss.finish(c);
+  }
+  // otherwise: pack into one staging buffer (one copy each way)
   size_t total = 0;
   for (size_t t = 0; t < count; ++t) total += 2 * nn[t];
   TRY(ensure(g.stage_b, total * sizeof(double)));
@@ -1062,6 +1098,7 @@ int gbfft_twofft(const double* data1, const double* data2, double* fft1, double*
   Call c(opts);
   TRY(check_form(c));
   if (!data1 || !data2 || !fft1 || !fft2) return fail(GBFFT_INVALID_ARG, "twofft: null pointer");
+  TRY(dev_aligned(c, "twofft", {fft1, fft2}));
   if (!is_pow2(n) || ilog2(n) > kMaxAxisLog)
     return fail(GBFFT_UNSUPPORTED_SIZE, "twofft: n=%zu must be a power of two", n);
   TRY(init_locked(g.device));
@@ -1100,6 +1137,7 @@ int gbfft_realft(double* data, size_t n, int isign, const gbfft_opts* opts) {
   Call c(opts);
   TRY(check_form(c));
   if (!data) return fail(GBFFT_INVALID_ARG, "realft: null data");
+  TRY(dev_aligned(c, "realft", {data}));
   TRY(check_isign(isign));
   if (n < 2 || !is_pow2(n) || ilog2(n) > kMaxAxisLog)
     return fail(GBFFT_UNSUPPORTED_SIZE, "realft: n=%zu must be a power of two >= 2", n);
@@ -1123,6 +1161,7 @@ int gbfft_fourn(double* data, const size_t* nn, size_t nn_len, size_t ndim, int 
   for (size_t i = 0; i < ndim; ++i)
     if (nn[i] <= 1) return fail(GBFFT_INVALID_ARG, "fourn: invalid dimension size");
   if (!data) return fail(GBFFT_INVALID_ARG, "fourn: null data");
+  TRY(dev_aligned(c, "fourn", {data}));
   long long dims[16];
   if (ndim > 16) return fail(GBFFT_UNSUPPORTED_SIZE, "fourn: ndim > 16");
   size_t total = 1;
@@ -1147,6 +1186,7 @@ int gbfft_rlft3(double* data, double* speq, size_t nn1, size_t nn2, size_t nn3, 
   Call c(opts);
   TRY(check_form(c));
   if (!data || !speq) return fail(GBFFT_INVALID_ARG, "rlft3: null pointer");
+  TRY(dev_aligned(c, "rlft3", {data, speq}));
   if (isign != 1 && isign != -1) return fail(GBFFT_INVALID_ARG, "rlft3: isign must be 1 or -1");
   if (!is_pow2(nn1) || !is_pow2(nn2) || !is_pow2(nn3) || nn3 < 2 ||
       ilog2(nn1) > kMaxAxisLog || ilog2(nn2) > kMaxAxisLog || ilog2(nn3) > kMaxAxisLog)
@@ -1180,8 +1220,10 @@ static int spectral_call(const Call& c, int kind, const double* a, const double*
                          size_t m, double* ans) {
   TRY(init_locked(g.device));
   StreamScope ss(c);
-  if (!c.dev() && n >= 4 && direct_fits((long long)n / 2, 2, c.form()) &&
-      direct_fits((long long)n / 2, 1, c.form())) {
+  // the direct path moves the data (and correl's second input) and the answer
+  // as 16-byte vectors
+  if (!c.dev() && n >= 4 && al16(a) && al16(ans) && (kind != 2 || al16(b)) &&
+      direct_fits((long long)n / 2, 2, c.form()) && direct_fits((long long)n / 2, 1, c.form())) {
     TRY(spectral_direct(c.form(), kind, a, b, (long long)n, (long long)m, ans));
     return ss.finish(c);
   }
@@ -1349,6 +1391,7 @@ static int spectrum_call(int kind, const double* cdata, size_t nn, double* out,
   std::lock_guard<std::mutex> lk(g_mu);
   Call c(opts);
   if (!cdata || !out) return fail(GBFFT_INVALID_ARG, "spectrum: null pointer");
+  TRY(dev_aligned(c, "spectrum", {cdata}));
   if (nn == 0) return GBFFT_OK;
   TRY(init_locked(g.device));
   StreamScope ss(c);
@@ -1383,6 +1426,7 @@ static Form trig_form(Form f) { return f == FORM_DF64 ? FORM_F64 : f; }
 static int trig_check(const Call& c, double* y, size_t n, const char* what) {
   TRY(check_form(c));
   if (!y) return fail(GBFFT_INVALID_ARG, "%s: null data", what);
+  TRY(dev_aligned(c, what, {y}));
   if (n < 2 || !is_pow2(n) || ilog2(n) > kMaxAxisLog - 2)
     return fail(GBFFT_UNSUPPORTED_SIZE, "%s: n=%zu must be a power of two >= 2", what, n);
   return GBFFT_OK;

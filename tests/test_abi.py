@@ -84,3 +84,26 @@ def test_python_mirror_raises_reference_errors(lib):
         nr.fourn(np.zeros(4), [1], 1, 1)
     with pytest.raises(ValueError):
         nr.cosft2(np.zeros(8), 8, 0)
+
+
+def test_unaligned_device_arrays_are_rejected_before_any_launch(lib):
+    """Device arrays must start on a 16-byte boundary (the kernels move complex
+    values as 16-byte vectors); an unaligned one is refused on the host, so no
+    GPU is needed to check it.  The pointers are never dereferenced."""
+    from numrs_gb300 import _lib as L
+    o = L.Opts()
+    o.form = 0
+    o.device_ptrs = 1
+    o.stream = None
+    o.async_ = 0
+    po = ctypes.byref(o)
+    bad = 0x7F0000001008  # 8-byte aligned only
+    assert lib.gbfft_four1(ctypes.c_void_p(bad), 8, 1, po) == L.INVALID_ARG
+    assert "16-byte" in L.last_error()
+    assert lib.gbfft_four1_many(ctypes.c_void_p(bad), 8, 2, 16, 1, po) == L.INVALID_ARG
+    assert lib.gbfft_realft(ctypes.c_void_p(bad), 8, 1, po) == L.INVALID_ARG
+    assert lib.gbfft_sinft(ctypes.c_void_p(bad), 8, po) == L.INVALID_ARG
+    ptrs = (ctypes.c_void_p * 2)(0x7F0000002000, bad)
+    nns = (ctypes.c_size_t * 2)(8, 8)
+    assert lib.gbfft_four1_batch(ptrs, nns, 2, 1, po) == L.INVALID_ARG
+    assert "16-byte" in L.last_error()

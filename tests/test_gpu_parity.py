@@ -446,3 +446,88 @@ def test_repeat_calls_bit_identical(nr):
     nr.four1(a, 1 << 15, 1)
     nr.four1(b, 1 << 15, 1)
     assert np.array_equal(a, b)
+
+
+def _unaligned(n):
+    """A float64 array of n values that starts 8 bytes past a 16-byte boundary
+    (as a Rust subslice data[1..] can)."""
+    buf = np.empty(n + 2)
+    off = 1 if buf.ctypes.data % 16 == 0 else 0
+    a = buf[off:off + n]
+    assert a.ctypes.data % 16 == 8
+    return a
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_unaligned_host_arrays(nr, form):
+    """Host arrays on an 8-byte boundary take the staged path (the direct host
+    path moves 16-byte vectors) and give the same results."""
+    nn = 4096
+    x = W.normal(900, 2 * nn)
+    a = _unaligned(2 * nn)
+    a[:] = x
+    nr.four1(a, nn, 1, form=form)
+    ref = x.copy()
+    O.four1(ref, nn, 1)
+    check(a, ref, 12, form, "unaligned four1")
+
+    n = 1 << 14
+    d = _unaligned(n)
+    d[:] = W.normal(901, n)
+    r = W.normal(902, 33)
+    out = _unaligned(n)
+    nr.convlv(d, r, 1, form=form, out=out)
+    st, ref = O.convlv(np.array(d), r, 1)
+    assert st == 0
+    check(out, ref, 14, form, "unaligned convlv")
+
+    e = _unaligned(n)
+    e[:] = W.normal(903, n)
+    out2 = _unaligned(n)
+    nr.correl(d, e, form=form, out=out2)
+    st, ref = O.correl(np.array(d), np.array(e))
+    assert st == 0
+    check(out2, ref, 14, form, "unaligned correl")
+
+    # a batch mixing aligned and unaligned arrays
+    sizes = [64, 8192, 256, 4096, 16384, 512]
+    pairs = []
+    for i, s in enumerate(sizes):
+        x = W.normal(910 + i, 2 * s)
+        arr = _unaligned(2 * s) if i % 2 else np.empty(2 * s)
+        arr[:] = x
+        pairs.append((x, arr))
+    nr.FFTProcessor(form=form).fft_batch([arr for _, arr in pairs], -1)
+    for (x, arr), s in zip(pairs, sizes):
+        ref = x.copy()
+        O.four1(ref, s, -1)
+        check(arr, ref, s.bit_length() - 1, form, "unaligned batch nn=%d" % s)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_batch_host_arrays_direct(nr, form):
+    """Aligned host arrays within the persistent limit are read and written in
+    place by the batched kernel; a repeat call replays the cached plan."""
+    sizes = [64, 8192, 128, 16384, 4096, 256, 2, 1, 8192, 512] * 3
+    data = [W.normal(950 + i, 2 * s) for i, s in enumerate(sizes)]
+    work = [np.empty(2 * s) for s in sizes]
+    assert all(w.ctypes.data % 16 == 0 for w in work)
+    proc = nr.FFTProcessor(form=form)
+    for rep in range(2):
+        for w, x in zip(work, data):
+            w[:] = x
+        proc.fft_batch(work, 1)
+        for w, x, s in zip(work, data, sizes):
+            ref = x.copy()
+            O.four1(ref, s, 1)
+            check(w, ref, max(1, s.bit_length() - 1), form, "direct batch nn=%d rep %d" % (s, rep))
+
+
+def test_unaligned_device_tensor_is_rejected(nr):
+    torch = pytest.importorskip("torch")
+    t = torch.zeros(2 * 64 + 1, dtype=torch.float64, device="cuda")
+    v = t[1:]
+    assert v.data_ptr() % 16 == 8
+    with pytest.raises(nr.GbfftError) as ei:
+        nr.four1(v, 64, 1)
+    assert "16-byte" in str(ei.value)
