@@ -16,8 +16,12 @@
  * Every function returns a gbfft_status.  Pointers are host memory unless
  * opts->device_ptrs is set.  Calls are synchronous for host pointers; for
  * device pointers they are ordered on opts->stream (NULL = the default
- * stream) and synchronous unless opts->async is set.  The library is thread-safe
- * (one internal lock).  No entry point changes any GPU setting.
+ * stream) and synchronous unless opts->async is set.  Device arrays that a
+ * transform works on in place must start on a 16-byte boundary (cudaMalloc
+ * memory always does); an unaligned one is rejected with GBFFT_INVALID_ARG
+ * before any launch.  Host arrays may start on any 8-byte boundary.  The
+ * library is thread-safe (one internal lock).  No entry point changes any GPU
+ * setting.
  */
 #ifndef GBFFT_H
 #define GBFFT_H
@@ -97,7 +101,8 @@ int gbfft_four1_batch(double* const* ptrs, const size_t* nn, size_t count, int i
  * callers that cannot call cudaMalloc when they need a transform (code running
  * under CUDA graph capture, hosts with a fixed memory budget, plugins inside
  * another framework's memory pool).  Same transform as gbfft_four1 in FP64,
- * in place on DEVICE memory `data`, ordered on `stream` (NULL = default).
+ * in place on DEVICE memory `data` (16-byte aligned), ordered on `stream`
+ * (NULL = default).
  * Its scratch and twiddle tables are fixed arrays in the library image (about
  * 19 MiB held by every GPU that loads the library, until exit), so nn is
  * limited to 2^20 (GBFFT_UNSUPPORTED_SIZE above).  The first call on a device

@@ -13,7 +13,8 @@
 // Limits and rules:
 //   - nn is a power of two with nn <= 2^20; larger sizes are rejected with
 //     GBFFT_UNSUPPORTED_SIZE (they would need more scratch than the array has)
-//   - data is device memory; the transform is in place, FP64, on `stream`
+//   - data is device memory on a 16-byte boundary; the transform is in place,
+//     FP64, on `stream`
 //   - the first call on a device sets that device up (looks up the arrays'
 //     device addresses and fills the twiddle table, then waits for the fill);
 //     make that first call before any stream capture
@@ -147,6 +148,11 @@ extern "C" int gbfft_four1_noalloc(double* data, size_t nn, int isign, void* str
   }
   if (isign != 1 && isign != -1) {
     record_error(GBFFT_INVALID_ARG, "four1_noalloc: isign must be 1 or -1");
+    return GBFFT_INVALID_ARG;
+  }
+  if (((uintptr_t)data) & 15u) {
+    // the passes move complex values as 16-byte vectors
+    record_error(GBFFT_INVALID_ARG, "four1_noalloc: device arrays must start on a 16-byte boundary");
     return GBFFT_INVALID_ARG;
   }
   if (nn == 0 || (nn & (nn - 1)) || nn > (size_t(1) << kNoAllocMaxLog)) {

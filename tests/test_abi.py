@@ -107,3 +107,5 @@ def test_unaligned_device_arrays_are_rejected_before_any_launch(lib):
     nns = (ctypes.c_size_t * 2)(8, 8)
     assert lib.gbfft_four1_batch(ptrs, nns, 2, 1, po) == L.INVALID_ARG
     assert "16-byte" in L.last_error()
+    assert lib.gbfft_four1_noalloc(ctypes.c_void_p(bad), 8, 1, None) == L.INVALID_ARG
+    assert "16-byte" in L.last_error()
