@@ -167,6 +167,25 @@ int gbfft_convlv(const double* data, size_t n, const double* respns, size_t m, i
 int gbfft_correl(const double* data1, size_t n1, const double* data2, size_t n2, double* ans,
                  const gbfft_opts* opts);
 
+/* convlv_batch: src/Convolve.rs:241
+ * `convlv_batch(data_batch: &[&[f64]], respns: &[f64], isign: i32)
+ *   -> Result<Vec<Array1<f64>>, ConvlvError>` (also ConvlvProcessor::process_batch,
+ * Convolve.rs:333).  `count` arrays data[i] of n[i] reals share one response of
+ * m taps; ans[i] receives n[i] reals.  convlv's checks run item by item in
+ * index order and the first failure is returned before any work.  Items of
+ * equal length are transformed together and share one response spectrum. */
+int gbfft_convlv_batch(const double* const* data, const size_t* n, size_t count,
+                       const double* respns, size_t m, int isign, double* const* ans,
+                       const gbfft_opts* opts);
+
+/* correl_batch: src/Correlation.rs:273
+ * `correl_batch(data_pairs: &[(&[f64], &[f64])]) -> Result<Vec<Array1<f64>>, CorrelError>`.
+ * Pair i is (data1[i], n1[i]), (data2[i], n2[i]); ans[i] receives n1[i]
+ * values.  correl's checks run item by item in index order. */
+int gbfft_correl_batch(const double* const* data1, const size_t* n1, const double* const* data2,
+                       const size_t* n2, size_t count, double* const* ans,
+                       const gbfft_opts* opts);
+
 /* correl_normalized: src/Correlation.rs:189 (fast = 0: two-pass statistics) and
  * correl_normalized_fast: :226 (fast = 1: one-pass sums; n <= 32 direct).
  * Inputs are standardised with their mean and population standard deviation,

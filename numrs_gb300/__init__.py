@@ -428,7 +428,9 @@ class ConvlvProcessor:
         return convlv(data, respns, isign, self.form)
 
     def process_batch(self, data_batch, respns, isign):
-        return [self.process(d, respns, isign) for d in data_batch]
+        """``process_batch`` (src/Convolve.rs:333): every branch of process()
+        computes convlv, so the batch is one convlv_batch call."""
+        return convlv_batch(data_batch, respns, isign, self.form)
 
 
 class RealFTProcessor:
@@ -479,14 +481,57 @@ class TwoFFTProcessor:
             self.process(data1, data2, fft1, fft2)
 
 
+def _ptr_table(args):
+    return (ctypes.c_void_p * max(len(args), 1))(*[x.ptr for x in args])
+
+
+def _size_table(sizes):
+    return (ctypes.c_size_t * max(len(sizes), 1))(*sizes)
+
+
 def convlv_batch(data_batch, respns, isign, form="fp64"):
-    """``convlv_batch`` (src/Convolve.rs:241)."""
-    return [convlv(d, respns, isign, form) for d in data_batch]
+    """``convlv_batch`` (src/Convolve.rs:241): one library call for the whole
+    batch; items of equal length share one response spectrum.  Raises the
+    ConvlvError of the first failing item."""
+    if len(data_batch) == 0:
+        return []
+    args = [_Arg(d, False) for d in data_batch]
+    r = _Arg(respns, False)
+    outs = [_new_like(a, a.size) for a in args]
+    oargs = [_Arg(o, True) for o in outs]
+    o = _opts(args + [r], form)
+    st = _lib.load().gbfft_convlv_batch(_ptr_table(args), _size_table([a.size for a in args]),
+                                        len(args), r.ptr, r.size, isign, _ptr_table(oargs),
+                                        ctypes.byref(o))
+    if st == _lib.EMPTY_INPUT:
+        raise ConvlvError.EmptyInput(_lib.last_error())
+    if st == _lib.RESPONSE_TOO_LONG:
+        raise ConvlvError.ResponseTooLong(_lib.last_error())
+    if st == _lib.INVALID_ISIGN:
+        raise ConvlvError.InvalidIsign(_lib.last_error())
+    _check(st)
+    return outs
 
 
 def correl_batch(pairs, form="fp64"):
-    """``correl_batch`` (src/Correlation.rs:273)."""
-    return [correl(a, b, form) for a, b in pairs]
+    """``correl_batch`` (src/Correlation.rs:273): one library call for all
+    pairs.  Raises the CorrelError of the first failing pair."""
+    if len(pairs) == 0:
+        return []
+    a1 = [_Arg(a, False) for a, _ in pairs]
+    a2 = [_Arg(b, False) for _, b in pairs]
+    outs = [_new_like(a, a.size) for a in a1]
+    oargs = [_Arg(o, True) for o in outs]
+    o = _opts(a1 + a2, form)
+    st = _lib.load().gbfft_correl_batch(_ptr_table(a1), _size_table([a.size for a in a1]),
+                                        _ptr_table(a2), _size_table([a.size for a in a2]),
+                                        len(a1), _ptr_table(oargs), ctypes.byref(o))
+    if st == _lib.EMPTY_INPUT:
+        raise CorrelError.EmptyInput(_lib.last_error())
+    if st == _lib.LENGTH_MISMATCH:
+        raise CorrelError.LengthMismatch(_lib.last_error())
+    _check(st)
+    return outs
 
 
 def autocorrel(data, form="fp64"):

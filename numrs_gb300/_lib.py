@@ -49,6 +49,8 @@ SIGNATURES = {
     "gbfft_cosft2": [_vp, _sz, ctypes.c_int, _op],
     "gbfft_convlv": [_vp, _sz, _vp, _sz, ctypes.c_int, _vp, _op],
     "gbfft_correl": [_vp, _sz, _vp, _sz, _vp, _op],
+    "gbfft_convlv_batch": [_vp, _vp, _sz, _vp, _sz, ctypes.c_int, _vp, _op],
+    "gbfft_correl_batch": [_vp, _vp, _vp, _vp, _sz, _vp, _op],
     "gbfft_correl_normalized": [_vp, _sz, _vp, _sz, _vp, ctypes.c_int, _op],
     "gbfft_magnitude_spectrum": [_vp, _sz, _vp, _op],
     "gbfft_power_spectrum": [_vp, _sz, _vp, _op],

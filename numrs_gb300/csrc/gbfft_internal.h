@@ -144,6 +144,11 @@ cudaError_t launch_realft_twist(Form f, int isign, double* data, long long n, lo
 // Writes the packed input of the inverse n/2-point FFT to out (may alias a).
 cudaError_t launch_spectral_product(Form f, int kind, const double* a, const double* b,
                                     double* out, long long n, Twiddles tw, cudaStream_t st);
+// The same step on `lines` lines whose a, b, out are sa, sb, so doubles apart
+// (sb = 0: one shared response spectrum).
+cudaError_t launch_spectral_lines(Form f, int kind, const double* a, long long sa,
+                                  const double* b, long long sb, double* out, long long so,
+                                  long long lines, long long n, Twiddles tw, cudaStream_t st);
 // Numerical Recipes wrap-around expansion of an m-tap response into n reals;
 // also copies `data` (n reals) to dst_data when non-null.
 cudaError_t launch_expand_response(const double* respns, long long m, double* dst, long long n,

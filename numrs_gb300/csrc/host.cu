@@ -1267,6 +1267,26 @@ int gbfft_convlv(const double* data, size_t n, const double* respns, size_t m, i
   return spectral_call(c, isign == 1 ? 0 : 1, data, respns, n, m, ans);
 }
 
+// The reference's direct linear branch for n <= 32 (src/Correlation.rs:19,37-50).
+static int correl_small(const Call& c, const double* data1, const double* data2, size_t n,
+                        double* ans) {
+  const double *a = data1, *b = data2;
+  double* out = ans;
+  if (!c.dev()) {
+    TRY(ensure(g.stage_c, 3 * n * sizeof(double)));
+    double* in = (double*)g.stage_c.p;
+    TRY(h2d(in, data1, n * sizeof(double)));
+    TRY(h2d(in + n, data2, n * sizeof(double)));
+    a = in;
+    b = in + n;
+    out = in + 2 * n;
+  }
+  CK(launch_correl_direct(a, b, out, (long long)n, g.cur));
+  g.launches++;
+  if (!c.dev()) TRY(d2h(ans, out, n * sizeof(double)));
+  return GBFFT_OK;
+}
+
 int gbfft_correl(const double* data1, size_t n1, const double* data2, size_t n2, double* ans,
                  const gbfft_opts* opts) {
   std::lock_guard<std::mutex> lk(g_mu);
@@ -1279,25 +1299,165 @@ int gbfft_correl(const double* data1, size_t n1, const double* data2, size_t n2,
   if (n <= 32) {
     TRY(init_locked(g.device));
     StreamScope ss(c);
-    const double *a = data1, *b = data2;
-    double* out = ans;
-    if (!c.dev()) {
-      TRY(ensure(g.stage_c, 3 * n * sizeof(double)));
-      double* in = (double*)g.stage_c.p;
-      TRY(h2d(in, data1, n * sizeof(double)));
-      TRY(h2d(in + n, data2, n * sizeof(double)));
-      a = in;
-      b = in + n;
-      out = in + 2 * n;
-    }
-    CK(launch_correl_direct(a, b, out, (long long)n, g.cur));
-    g.launches++;
-    if (!c.dev()) TRY(d2h(ans, out, n * sizeof(double)));
+    TRY(correl_small(c, data1, data2, n, ans));
     return ss.finish(c);
   }
   if (!is_pow2(n) || ilog2(n) > kMaxAxisLog)
     return fail(GBFFT_UNSUPPORTED_SIZE, "correl: n=%zu must be a power of two when > 32", n);
   return spectral_call(c, 2, data1, data2, n, n, ans);
+}
+
+// ---------------------------------------------------------------------------
+// Batched convolution and correlation (src/Convolve.rs:241 convlv_batch and
+// ConvlvProcessor::process_batch :333; src/Correlation.rs:273 correl_batch).
+// Items of equal length are transformed together: one batched forward FFT of
+// all their lines, one spectral launch over all lines, one batched inverse
+// FFT.  For convlv the response spectrum is computed once per length and
+// shared by every item.
+// ---------------------------------------------------------------------------
+namespace {
+
+int load_line(const Call& c, double* dst, const double* src, size_t doubles) {
+  return c.dev() ? d2d(dst, src, doubles * sizeof(double)) : h2d(dst, src, doubles * sizeof(double));
+}
+int store_line(const Call& c, double* dst, const double* src, size_t doubles) {
+  return c.dev() ? d2d(dst, src, doubles * sizeof(double)) : d2h(dst, src, doubles * sizeof(double));
+}
+
+// item indices grouped by length, groups in increasing length, items in order
+std::map<size_t, std::vector<size_t>> by_length(const size_t* n, size_t count) {
+  std::map<size_t, std::vector<size_t>> groups;
+  for (size_t i = 0; i < count; ++i) groups[n[i]].push_back(i);
+  return groups;
+}
+
+// lines per chunk of one group: at most 2^27 doubles (1 GiB) of work space
+size_t lines_per_chunk(size_t n, size_t reserved_lines) {
+  const size_t cap = ((size_t)1 << 27) / n;
+  return cap > reserved_lines + 1 ? cap - reserved_lines : 1;
+}
+
+int convlv_group(const Call& c, const std::vector<size_t>& items, const double* const* data,
+                 size_t n, const double* rdev, size_t m, int kind, double* const* ans) {
+  const Form f = c.form();
+  Twiddles tw;
+  TRY(tables(f, tw));
+  const long long nh = (long long)n / 2;
+  const size_t per = lines_per_chunk(n, 1);
+  for (size_t i0 = 0; i0 < items.size(); i0 += per) {
+    const size_t cnt = std::min(per, items.size() - i0);
+    TRY(ensure(g.work, (cnt + 1) * n * sizeof(double)));
+    double* w = (double*)g.work.p;  // [response | data 0 | data 1 | ...]
+    CK(launch_expand_response(rdev, (long long)m, w, (long long)n, nullptr, nullptr, g.cur));
+    g.launches++;
+    for (size_t j = 0; j < cnt; ++j) TRY(load_line(c, w + (j + 1) * n, data[items[i0 + j]], n));
+    TRY(fft_lines(f, 1, w, nh, (long long)cnt + 1, nh));
+    {
+      ProfScope ps(PK_SPECTRAL, 3.0 * (double)n * 8 * (double)cnt);
+      CK(launch_spectral_lines(f, kind, w + n, (long long)n, w, 0, w + n, (long long)n,
+                               (long long)cnt, (long long)n, tw, g.cur));
+    }
+    g.launches++;
+    TRY(fft_lines(f, -1, w + n, nh, (long long)cnt, nh));
+    for (size_t j = 0; j < cnt; ++j) TRY(store_line(c, ans[items[i0 + j]], w + (j + 1) * n, n));
+  }
+  return GBFFT_OK;
+}
+
+int correl_group(const Call& c, const std::vector<size_t>& items, const double* const* data1,
+                 const double* const* data2, size_t n, double* const* ans) {
+  const Form f = c.form();
+  Twiddles tw;
+  TRY(tables(f, tw));
+  const long long nh = (long long)n / 2;
+  const size_t per = std::max<size_t>(1, lines_per_chunk(n, 0) / 2);
+  for (size_t i0 = 0; i0 < items.size(); i0 += per) {
+    const size_t cnt = std::min(per, items.size() - i0);
+    TRY(ensure(g.work, 2 * cnt * n * sizeof(double)));
+    double* w = (double*)g.work.p;  // [data1 lines | data2 lines]
+    double* wb = w + cnt * n;
+    for (size_t j = 0; j < cnt; ++j) {
+      TRY(load_line(c, w + j * n, data1[items[i0 + j]], n));
+      TRY(load_line(c, wb + j * n, data2[items[i0 + j]], n));
+    }
+    TRY(fft_lines(f, 1, w, nh, 2 * (long long)cnt, nh));
+    {
+      ProfScope ps(PK_SPECTRAL, 3.0 * (double)n * 8 * (double)cnt);
+      CK(launch_spectral_lines(f, 2, w, (long long)n, wb, (long long)n, w, (long long)n,
+                               (long long)cnt, (long long)n, tw, g.cur));
+    }
+    g.launches++;
+    TRY(fft_lines(f, -1, w, nh, (long long)cnt, nh));
+    for (size_t j = 0; j < cnt; ++j) TRY(store_line(c, ans[items[i0 + j]], w + j * n, n));
+  }
+  return GBFFT_OK;
+}
+
+}  // namespace
+
+int gbfft_convlv_batch(const double* const* data, const size_t* n, size_t count,
+                       const double* respns, size_t m, int isign, double* const* ans,
+                       const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  if (count == 0) return GBFFT_OK;
+  if (!data || !n || !ans) return fail(GBFFT_INVALID_ARG, "convlv_batch: null arrays");
+  // convlv's checks (src/Convolve.rs:13-21), item by item in index order
+  for (size_t i = 0; i < count; ++i) {
+    if (n[i] == 0 || m == 0)
+      return fail(GBFFT_EMPTY_INPUT, "convlv_batch: item %zu: input arrays cannot be empty", i);
+    if (m > n[i])
+      return fail(GBFFT_RESPONSE_TOO_LONG, "convlv_batch: item %zu: response function longer than data", i);
+    if (isign != 1 && isign != -1)
+      return fail(GBFFT_INVALID_ISIGN, "convlv_batch: isign must be 1 (convolution) or -1 (deconvolution)");
+    if (!data[i] || !ans[i] || !respns)
+      return fail(GBFFT_INVALID_ARG, "convlv_batch: item %zu: null pointer", i);
+    if (n[i] < 2 || !is_pow2(n[i]) || ilog2(n[i]) > kMaxAxisLog)
+      return fail(GBFFT_UNSUPPORTED_SIZE, "convlv_batch: item %zu: n=%zu must be a power of two >= 2", i, n[i]);
+  }
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  const double* rdev = respns;
+  if (!c.dev()) {
+    TRY(ensure(g.stage_c, m * sizeof(double)));
+    TRY(h2d(g.stage_c.p, respns, m * sizeof(double)));
+    rdev = (const double*)g.stage_c.p;
+  }
+  for (auto& grp : by_length(n, count))
+    TRY(convlv_group(c, grp.second, data, grp.first, rdev, m, isign == 1 ? 0 : 1, ans));
+  return ss.finish(c);
+}
+
+int gbfft_correl_batch(const double* const* data1, const size_t* n1, const double* const* data2,
+                       const size_t* n2, size_t count, double* const* ans,
+                       const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  if (count == 0) return GBFFT_OK;
+  if (!data1 || !n1 || !data2 || !n2 || !ans)
+    return fail(GBFFT_INVALID_ARG, "correl_batch: null arrays");
+  // correl's checks (src/Correlation.rs:10-16), item by item in index order
+  for (size_t i = 0; i < count; ++i) {
+    if (n1[i] == 0) return fail(GBFFT_EMPTY_INPUT, "correl_batch: item %zu: input arrays cannot be empty", i);
+    if (n2[i] != n1[i])
+      return fail(GBFFT_LENGTH_MISMATCH, "correl_batch: item %zu: input arrays must have the same length", i);
+    if (!data1[i] || !data2[i] || !ans[i])
+      return fail(GBFFT_INVALID_ARG, "correl_batch: item %zu: null pointer", i);
+    if (n1[i] > 32 && (!is_pow2(n1[i]) || ilog2(n1[i]) > kMaxAxisLog))
+      return fail(GBFFT_UNSUPPORTED_SIZE, "correl_batch: item %zu: n=%zu must be a power of two when > 32", i, n1[i]);
+  }
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  for (auto& grp : by_length(n1, count)) {
+    if (grp.first <= 32) {
+      for (size_t i : grp.second) TRY(correl_small(c, data1[i], data2[i], grp.first, ans[i]));
+    } else {
+      TRY(correl_group(c, grp.second, data1, data2, grp.first, ans));
+    }
+  }
+  return ss.finish(c);
 }
 
 // correl_normalized (fast = 0, src/Correlation.rs:189-223) and

@@ -200,10 +200,15 @@ __device__ __forceinline__ double spec_prod_real(double x, double y, double inv_
   }
 }
 
+// One line per blockIdx.y: lines of a, b and out are sa, sb, so doubles apart
+// (sb = 0 shares one response spectrum among all lines).
 template <class F, int KIND>
 __global__ void k_spectral(const double* a, const double* b, double* out, long long n,
-                           Twiddles tw) {
+                           Twiddles tw, long long sa, long long sb, long long so) {
   using C = typename F::C;
+  a += (long long)blockIdx.y * sa;
+  b += (long long)blockIdx.y * sb;
+  out += (long long)blockIdx.y * so;
   const long long nq = n / 4;
   const long long per = nq > 0 ? nq : 1;
   const double inv_no2 = 2.0 / (double)n;
@@ -245,22 +250,37 @@ __global__ void k_spectral(const double* a, const double* b, double* out, long l
   }
 }
 
-cudaError_t launch_spectral_product(Form f, int kind, const double* a, const double* b,
-                                    double* out, long long n, Twiddles tw, cudaStream_t st) {
+cudaError_t launch_spectral_lines(Form f, int kind, const double* a, long long sa,
+                                  const double* b, long long sb, double* out, long long so,
+                                  long long lines, long long n, Twiddles tw, cudaStream_t st) {
   long long work = n / 4 + 1;
   int blocks = (int)((work + 255) / 256);
   if (blocks > 152 * 16) blocks = 152 * 16;
-#define SP_LAUNCH(FT)                                                                      \
-  switch (kind) {                                                                          \
-    case 0: k_spectral<FT, 0><<<blocks, 256, 0, st>>>(a, b, out, n, tw); break;            \
-    case 1: k_spectral<FT, 1><<<blocks, 256, 0, st>>>(a, b, out, n, tw); break;            \
-    default: k_spectral<FT, 2><<<blocks, 256, 0, st>>>(a, b, out, n, tw); break;           \
+  for (long long l0 = 0; l0 < lines; l0 += 65535) {
+    const unsigned ny = (unsigned)(lines - l0 < 65535 ? lines - l0 : 65535);
+    const dim3 grid((unsigned)blocks, ny);
+    const double* al = a + l0 * sa;
+    const double* bl = b + l0 * sb;
+    double* ol = out + l0 * so;
+#define SP_LAUNCH(FT)                                                                           \
+  switch (kind) {                                                                               \
+    case 0: k_spectral<FT, 0><<<grid, 256, 0, st>>>(al, bl, ol, n, tw, sa, sb, so); break;      \
+    case 1: k_spectral<FT, 1><<<grid, 256, 0, st>>>(al, bl, ol, n, tw, sa, sb, so); break;      \
+    default: k_spectral<FT, 2><<<grid, 256, 0, st>>>(al, bl, ol, n, tw, sa, sb, so); break;     \
   }
-  if (f == FORM_F64) { SP_LAUNCH(F64) }
-  else if (f == FORM_F32 || f == FORM_TC32) { SP_LAUNCH(F32) }
-  else { SP_LAUNCH(DF64) }
+    if (f == FORM_F64) { SP_LAUNCH(F64) }
+    else if (f == FORM_F32 || f == FORM_TC32) { SP_LAUNCH(F32) }
+    else { SP_LAUNCH(DF64) }
 #undef SP_LAUNCH
-  return cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_spectral_product(Form f, int kind, const double* a, const double* b,
+                                    double* out, long long n, Twiddles tw, cudaStream_t st) {
+  return launch_spectral_lines(f, kind, a, 0, b, 0, out, 0, 1, n, tw, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -109,3 +109,28 @@ def test_unaligned_device_arrays_are_rejected_before_any_launch(lib):
     assert "16-byte" in L.last_error()
     assert lib.gbfft_four1_noalloc(ctypes.c_void_p(bad), 8, 1, None) == L.INVALID_ARG
     assert "16-byte" in L.last_error()
+
+
+def test_batch_wrapper_errors_need_no_gpu(lib):
+    """convlv_batch / correl_batch run convlv's and correl's checks item by item
+    and return the first failure before any work."""
+    from numrs_gb300 import _lib as L
+    x = np.zeros(8)
+    p = x.ctypes.data
+    ptrs = (ctypes.c_void_p * 2)(p, p)
+    outs = (ctypes.c_void_p * 2)(p, p)
+    ns = (ctypes.c_size_t * 2)(8, 0)
+    assert lib.gbfft_convlv_batch(ptrs, ns, 2, p, 3, 1, outs, None) == L.EMPTY_INPUT
+    assert "item 1" in L.last_error()
+    ns = (ctypes.c_size_t * 2)(8, 2)
+    assert lib.gbfft_convlv_batch(ptrs, ns, 2, p, 3, 1, outs, None) == L.RESPONSE_TOO_LONG
+    ns = (ctypes.c_size_t * 2)(8, 8)
+    assert lib.gbfft_convlv_batch(ptrs, ns, 2, p, 3, 0, outs, None) == L.INVALID_ISIGN
+    ns = (ctypes.c_size_t * 2)(8, 6)
+    assert lib.gbfft_convlv_batch(ptrs, ns, 2, p, 3, 1, outs, None) == L.UNSUPPORTED_SIZE
+    n1 = (ctypes.c_size_t * 2)(8, 8)
+    n2 = (ctypes.c_size_t * 2)(8, 7)
+    assert lib.gbfft_correl_batch(ptrs, n1, ptrs, n2, 2, outs, None) == L.LENGTH_MISMATCH
+    n1 = (ctypes.c_size_t * 2)(0, 8)
+    assert lib.gbfft_correl_batch(ptrs, n1, ptrs, n1, 2, outs, None) == L.EMPTY_INPUT
+    assert lib.gbfft_convlv_batch(ptrs, ns, 0, p, 3, 1, outs, None) == L.OK

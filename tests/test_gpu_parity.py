@@ -2,7 +2,10 @@
 
 Bars (written into each check):
   FP64 and DF64 forms: rel-L2 <= 1e-12 and max-abs <= 1e-12 * ||X_ref||_inf * log2 N
-  FP32 and tensor-core (3xTF32) forms: rel-L2 <= 1e-6
+  FP32 and tensor-core (3xTF32) forms: rel-L2 <= 1e-6 per transform.  A
+  convolution or correlation is three transforms in sequence (two forward, one
+  inverse) whose independent errors add in quadrature, so its bar is
+  sqrt(3) * 1e-6 (check_composite).
 """
 import os
 
@@ -31,6 +34,17 @@ def check(got, ref, log2n, form, what=""):
     if form in ("fp32", "tc32"):
         e = rel_l2(got, ref)
         assert e <= 1e-6, "%s %s rel-L2 %.3e > 1e-6" % (what, form, e)
+    else:
+        assert_fp64_close(got, ref, log2n, "%s %s" % (what, form))
+
+
+def check_composite(got, ref, log2n, form, what="", transforms=3):
+    """Bar of a result made of `transforms` transforms in sequence: FP64/DF64 as
+    check(); FP32/TC32 at sqrt(transforms) * 1e-6 rel-L2."""
+    if form in ("fp32", "tc32"):
+        bar = 1e-6 * transforms ** 0.5
+        e = rel_l2(got, ref)
+        assert e <= bar, "%s %s rel-L2 %.3e > %.2e" % (what, form, e, bar)
     else:
         assert_fp64_close(got, ref, log2n, "%s %s" % (what, form))
 
@@ -260,10 +274,10 @@ def test_convlv(nr, form, n, m):
     got = nr.convlv(x, r, 1, form=form)
     st, ref = O.convlv(x, r, 1)
     assert st == 0
-    check(got, ref, max(1, n.bit_length() - 1), form, "convlv n=%d m=%d" % (n, m))
+    check_composite(got, ref, max(1, n.bit_length() - 1), form, "convlv n=%d m=%d" % (n, m))
     got2 = nr.convlv(ref, r, -1, form=form)
     st, ref2 = O.convlv(ref, r, -1)
-    check(got2, ref2, max(1, n.bit_length() - 1), form, "deconvolve n=%d m=%d" % (n, m))
+    check_composite(got2, ref2, max(1, n.bit_length() - 1), form, "deconvolve n=%d m=%d" % (n, m))
 
 
 @pytest.mark.parametrize("form", FORMS)
@@ -273,7 +287,7 @@ def test_convlv_c2_full_size(nr, form):
     got = nr.convlv(x, r, 1, form=form)
     st, ref = O.convlv(x, r, 1)
     assert st == 0
-    check(got, ref, 20, form, "convlv C2")
+    check_composite(got, ref, 20, form, "convlv C2")
 
 
 def test_convlv_golden(nr):
@@ -291,7 +305,7 @@ def test_correl(nr, form, n):
     got = nr.correl(a, b, form=form)
     st, ref = O.correl(a, b)
     assert st == 0
-    check(got, ref, max(1, n.bit_length() - 1), form, "correl n=%d" % n)
+    check_composite(got, ref, max(1, n.bit_length() - 1), form, "correl n=%d" % n)
 
 
 def test_correl_kats(nr):
@@ -479,7 +493,7 @@ def test_unaligned_host_arrays(nr, form):
     nr.convlv(d, r, 1, form=form, out=out)
     st, ref = O.convlv(np.array(d), r, 1)
     assert st == 0
-    check(out, ref, 14, form, "unaligned convlv")
+    check_composite(out, ref, 14, form, "unaligned convlv")
 
     e = _unaligned(n)
     e[:] = W.normal(903, n)
@@ -487,7 +501,7 @@ def test_unaligned_host_arrays(nr, form):
     nr.correl(d, e, form=form, out=out2)
     st, ref = O.correl(np.array(d), np.array(e))
     assert st == 0
-    check(out2, ref, 14, form, "unaligned correl")
+    check_composite(out2, ref, 14, form, "unaligned correl")
 
     # a batch mixing aligned and unaligned arrays
     sizes = [64, 8192, 256, 4096, 16384, 512]
@@ -531,3 +545,54 @@ def test_unaligned_device_tensor_is_rejected(nr):
     with pytest.raises(nr.GbfftError) as ei:
         nr.four1(v, 64, 1)
     assert "16-byte" in str(ei.value)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_convlv_batch_shared_response(nr, form):
+    """convlv_batch over items of mixed lengths (one shared response spectrum per
+    length) against the oracle's convlv of each item; deconvolution of the
+    results gives the inputs back."""
+    lengths = [1024, 4096, 1024, 1 << 16, 16, 8, 4096, 1024]
+    data = [W.normal(1200 + i, n) for i, n in enumerate(lengths)]
+    r = W.normal(1300, 7)
+    got = nr.convlv_batch(data, r, 1, form=form)
+    assert len(got) == len(data)
+    for x, y, n in zip(data, got, lengths):
+        st, ref = O.convlv(x, r, 1)
+        assert st == 0
+        check_composite(y, ref, max(1, n.bit_length() - 1), form, "convlv_batch n=%d" % n)
+    back = nr.ConvlvProcessor(form=form).process_batch(
+        [np.asarray(y) for y in got], r, -1)
+    for y, b, n in zip(got, back, lengths):
+        st, ref = O.convlv(np.asarray(y), r, -1)
+        check_composite(b, ref, max(1, n.bit_length() - 1), form, "deconvolve batch n=%d" % n)
+
+
+def test_convlv_batch_device_and_errors(nr):
+    torch = pytest.importorskip("torch")
+    lengths = [2048, 2048, 512]
+    data = [W.normal(1400 + i, n) for i, n in enumerate(lengths)]
+    r = W.normal(1500, 31)
+    got = nr.convlv_batch([torch.from_numpy(x).cuda() for x in data], torch.from_numpy(r).cuda(), 1)
+    for x, y, n in zip(data, got, lengths):
+        st, ref = O.convlv(x, r, 1)
+        assert_fp64_close(y.cpu().numpy(), ref, n.bit_length() - 1, "device convlv_batch")
+    with pytest.raises(nr.ConvlvError.ResponseTooLong):
+        nr.convlv_batch([data[0], np.zeros(16)], r, 1)
+    with pytest.raises(nr.ConvlvError.EmptyInput):
+        nr.convlv_batch([data[0], np.zeros(0)], r, 1)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_correl_batch(nr, form):
+    """correl_batch over pairs of mixed lengths, including the direct n <= 32
+    branch, against the oracle's correl of each pair."""
+    lengths = [1, 5, 32, 64, 4096, 64, 1 << 15, 32]
+    pairs = [(W.normal(1600 + i, n), W.normal(1700 + i, n)) for i, n in enumerate(lengths)]
+    got = nr.correl_batch(pairs, form=form)
+    for (a, b), y, n in zip(pairs, got, lengths):
+        st, ref = O.correl(a, b)
+        assert st == 0
+        check_composite(y, ref, max(1, n.bit_length() - 1), form, "correl_batch n=%d" % n)
+    with pytest.raises(nr.CorrelError.LengthMismatch):
+        nr.correl_batch([pairs[3], (np.ones(8), np.ones(9))], form=form)
