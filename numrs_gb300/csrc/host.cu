@@ -1216,10 +1216,34 @@ int gbfft_rlft3(double* data, double* speq, size_t nn1, size_t nn2, size_t nn3, 
   return ss.finish(c);
 }
 
+static int load_one(const Call& c, double* dst, const double* src, size_t doubles) {
+  return c.dev() ? d2d(dst, src, doubles * sizeof(double)) : h2d(dst, src, doubles * sizeof(double));
+}
+
 static int spectral_call(const Call& c, int kind, const double* a, const double* b, size_t n,
                          size_t m, double* ans) {
   TRY(init_locked(g.device));
   StreamScope ss(c);
+  if (kind == 2 && a == b) {
+    // autocorrelation (src/Correlation.rs:281-286): one forward transform, its
+    // spectrum used as both operands of the conjugate product
+    Twiddles tw;
+    TRY(tables(c.form(), tw));
+    TRY(ensure(g.work, n * sizeof(double)));
+    double* w = (double*)g.work.p;
+    TRY(load_one(c, w, a, n));
+    const long long nh = (long long)n / 2;
+    TRY(fft_lines(c.form(), 1, w, nh, 1, nh));
+    {
+      ProfScope ps(PK_SPECTRAL, 2.0 * n * 8);
+      CK(launch_spectral_product(c.form(), 2, w, w, w, (long long)n, tw, g.cur));
+    }
+    g.launches++;
+    TRY(fft_lines(c.form(), -1, w, nh, 1, nh));
+    if (c.dev()) TRY(d2d(ans, w, n * sizeof(double)));
+    else TRY(d2h(ans, w, n * sizeof(double)));
+    return ss.finish(c);
+  }
   // the direct path moves the data (and correl's second input) and the answer
   // as 16-byte vectors
   if (!c.dev() && n >= 4 && al16(a) && al16(ans) && (kind != 2 || al16(b)) &&

@@ -596,3 +596,22 @@ def test_correl_batch(nr, form):
         check_composite(y, ref, max(1, n.bit_length() - 1), form, "correl_batch n=%d" % n)
     with pytest.raises(nr.CorrelError.LengthMismatch):
         nr.correl_batch([pairs[3], (np.ones(8), np.ones(9))], form=form)
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("n", [16, 64, 4096, 1 << 20])
+def test_autocorrel(nr, form, n):
+    """autocorrel / autocorrel_fast (src/Correlation.rs:281-286): one forward
+    transform whose spectrum is both operands, against the oracle's correl(x, x)."""
+    x = W.normal(1800 + n, n)
+    st, ref = O.correl(x, x)
+    assert st == 0
+    check_composite(nr.autocorrel(x, form=form), ref, max(1, n.bit_length() - 1), form,
+                    "autocorrel n=%d" % n, transforms=2)
+    check_composite(nr.autocorrel_fast(x, form=form), ref, max(1, n.bit_length() - 1), form,
+                    "autocorrel_fast n=%d" % n, transforms=2)
+    if form == "fp64":
+        torch = pytest.importorskip("torch")
+        xd = torch.from_numpy(x).cuda()
+        got = nr.autocorrel(xd).cpu().numpy()
+        assert_fp64_close(got, ref, max(1, n.bit_length() - 1), "device autocorrel n=%d" % n)
