@@ -194,7 +194,10 @@ int gbfft_correl_batch(const double* const* data1, const size_t* n1, const doubl
 int gbfft_correl_normalized(const double* data1, size_t n1, const double* data2, size_t n2,
                             double* ans, int fast, const gbfft_opts* opts);
 
-/* magnitude_spectrum / power_spectrum: src/FFT_1.rs:206,218.  out[nn]. */
+/* magnitude_spectrum / power_spectrum: src/FFT_1.rs:206,218.  c holds nn
+ * interleaved complex values; out[nn].  The crate maps chunks(2) of its slice,
+ * so for an odd-length slice it appends one 0.0 for the trailing half chunk:
+ * the binding passes nn = len / 2 and appends that entry. */
 int gbfft_magnitude_spectrum(const double* c, size_t nn, double* out, const gbfft_opts* opts);
 int gbfft_power_spectrum(const double* c, size_t nn, double* out, const gbfft_opts* opts);
 

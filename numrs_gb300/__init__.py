@@ -539,22 +539,28 @@ def autocorrel(data, form="fp64"):
     return correl(data, data, form)
 
 
-def magnitude_spectrum(c, form="fp64"):
+def _spectrum(fn, c, form):
+    """The crate maps chunks(2) of the input: an odd-length input ends with a
+    half chunk, whose entry is 0.0 (src/FFT_1.rs:206-228)."""
     a = _Arg(c, False)
-    out = _new_like(a, a.size // 2)
-    o = _opts([a], form)
-    _check(_lib.load().gbfft_magnitude_spectrum(a.ptr, a.size // 2, _Arg(out, True).ptr,
-                                                ctypes.byref(o)))
+    nn = a.size // 2
+    out = _new_like(a, nn + (a.size & 1))
+    if nn:
+        o = _opts([a], form)
+        _check(getattr(_lib.load(), fn)(a.ptr, nn, _Arg(out, True).ptr, ctypes.byref(o)))
+    if a.size & 1:
+        out[nn] = 0.0
     return out
+
+
+def magnitude_spectrum(c, form="fp64"):
+    """``magnitude_spectrum`` (src/FFT_1.rs:206): |c_k| of interleaved complex data."""
+    return _spectrum("gbfft_magnitude_spectrum", c, form)
 
 
 def power_spectrum(c, form="fp64"):
-    a = _Arg(c, False)
-    out = _new_like(a, a.size // 2)
-    o = _opts([a], form)
-    _check(_lib.load().gbfft_power_spectrum(a.ptr, a.size // 2, _Arg(out, True).ptr,
-                                            ctypes.byref(o)))
-    return out
+    """``power_spectrum`` (src/FFT_1.rs:218): |c_k|^2 of interleaved complex data."""
+    return _spectrum("gbfft_power_spectrum", c, form)
 
 
 def real_to_complex(x):

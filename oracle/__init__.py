@@ -159,14 +159,18 @@ def correl_normalized(data1, data2, fast=False):
 
 
 def magnitude_spectrum(c):
-    out = np.zeros(c.size // 2)
-    lib().orc_magnitude_spectrum(_ptr(c), c.size // 2, _ptr(out))
+    """``src/FFT_1.rs:206``: chunks(2); an odd-length input's last half chunk gives 0.0."""
+    out = np.zeros(c.size // 2 + (c.size & 1))
+    if c.size >= 2:
+        lib().orc_magnitude_spectrum(_ptr(c), c.size // 2, _ptr(out))
     return out
 
 
 def power_spectrum(c):
-    out = np.zeros(c.size // 2)
-    lib().orc_power_spectrum(_ptr(c), c.size // 2, _ptr(out))
+    """``src/FFT_1.rs:218``, as magnitude_spectrum."""
+    out = np.zeros(c.size // 2 + (c.size & 1))
+    if c.size >= 2:
+        lib().orc_power_spectrum(_ptr(c), c.size // 2, _ptr(out))
     return out
 
 

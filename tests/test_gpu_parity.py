@@ -418,6 +418,12 @@ def test_spectra(nr):
     p = nr.power_spectrum(x)
     assert_fp64_close(m, O.magnitude_spectrum(x), 10, "magnitude")
     assert_fp64_close(p, O.power_spectrum(x), 10, "power")
+    # odd length: the crate's chunks(2) ends with a half chunk, whose entry is 0.0
+    y = W.normal(10, 2049)
+    m = nr.magnitude_spectrum(y)
+    assert m.size == 1025 and m[-1] == 0.0
+    assert_fp64_close(m, O.magnitude_spectrum(y), 10, "magnitude, odd length")
+    assert list(nr.power_spectrum(np.array([3.0]))) == [0.0]
 
 
 def test_large_roundtrip_properties(nr):

@@ -269,3 +269,12 @@ def test_workload_generator_is_deterministic():
     sizes, u = W.batch_c3(count=2000)
     assert sizes.min() >= 64 and sizes.max() <= 1 << 14
     assert len(set(sizes.tolist())) == 9
+
+
+def test_spectrum_odd_length_matches_chunks():
+    """src/FFT_1.rs:206-228 map chunks(2): an odd-length input's trailing half
+    chunk contributes 0.0."""
+    c = np.array([3.0, 4.0, 1.0])
+    assert list(O.magnitude_spectrum(c)) == [5.0, 0.0]
+    assert list(O.power_spectrum(c)) == [25.0, 0.0]
+    assert list(O.power_spectrum(np.array([2.0]))) == [0.0]
