@@ -526,11 +526,33 @@ __device__ __forceinline__ void first_subpass(const PassParams& p, long long lin
     const unsigned jm = (unsigned)(jg & (p.Ns - 1));
     C v[Q];
 #pragma unroll
-    for (int t = 0; t < Q; ++t) {
-      v[t] = gload<F, IN>(&raw[i][t], 0);
-      const unsigned r = (unsigned)(j + (t << logRQ));
-      // jm * r < Ns * R <= L
-      if (p.logNs > 0 && jm != 0 && r != 0) v[t] = F::mul(v[t], twiddle<F>(p.tw, logS, jm * r, SG));
+    for (int t = 0; t < Q; ++t) v[t] = gload<F, IN>(&raw[i][t], 0);
+    if constexpr (F::kind == 1 && Q >= 4) {
+      // FP32: the twiddles w^(jm (j + t R/Q)), t = 4a + b, are products
+      // w^(jm (j + 4a R/Q)) * w^(jm b R/Q) of two correctly rounded table
+      // entries (one more rounding): Q/4 + 3 gathered table loads instead of Q.
+      // Every exponent is below jm * R <= Ns * R = 2^logS.
+      if (p.logNs > 0 && jm != 0) {
+        const unsigned base = jm * (unsigned)j, step = jm << logRQ;
+        C sb[4];
+        sb[0] = F::from_s(typename F::S{1.f, 0.f});
+#pragma unroll
+        for (int b = 1; b < 4; ++b) sb[b] = twiddle<F>(p.tw, logS, step * (unsigned)b, SG);
+#pragma unroll
+        for (int a = 0; a < Q / 4; ++a) {
+          const C la = twiddle<F>(p.tw, logS, base + step * (unsigned)(4 * a), SG);
+          v[4 * a] = F::mul(v[4 * a], la);
+#pragma unroll
+          for (int b = 1; b < 4; ++b) v[4 * a + b] = F::mul(v[4 * a + b], F::mul(la, sb[b]));
+        }
+      }
+    } else {
+#pragma unroll
+      for (int t = 0; t < Q; ++t) {
+        const unsigned r = (unsigned)(j + (t << logRQ));
+        // jm * r < Ns * R <= L
+        if (p.logNs > 0 && jm != 0 && r != 0) v[t] = F::mul(v[t], twiddle<F>(p.tw, logS, jm * r, SG));
+      }
     }
     dftq<F, SG, Q>(v);
     const int cb = c * cs;
