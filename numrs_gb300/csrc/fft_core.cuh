@@ -169,6 +169,14 @@ __device__ __forceinline__ void subpass(typename F::S* sm, int logR, int cs, int
   __syncthreads();
 }
 
+// Output scaling: the FP32-pipe forms use the float copy of the scale.
+template <class F>
+__device__ __forceinline__ typename F::C apply_scale(typename F::C w, const PassParams& p) {
+  if constexpr (F::kind == 1) return {w.x * p.fscale, w.y * p.fscale};
+  else if constexpr (F::kind == 2) return {df_scale_f(w.x, p.fscale), df_scale_f(w.y, p.fscale)};
+  else return F::scale(w, p.scale);
+}
+
 // ---------------------------------------------------------------------------
 // Global element access with format conversion.
 // ---------------------------------------------------------------------------
@@ -240,12 +248,10 @@ __device__ __forceinline__ void tile_origin(const PassParams& p, long long tile,
     line0 = tile >> logTpl;
     j0 = (tile & ((1ll << logTpl) - 1)) << p.logC;
   } else {
-    // tile < p.tiles < 2^31: a 32-bit division (64-bit integer division is a
-    // long software sequence that runs partly on the FP64 pipe)
-    const unsigned ng = (unsigned)((p.nlines + (1ll << p.logC) - 1) >> p.logC);
-    const unsigned jq = (unsigned)tile / ng;
-    j0 = jq;
-    line0 = (long long)((unsigned)tile - jq * ng) << p.logC;
+    // j0 fastest: L/R is a power of two, so no division (an integer division
+    // is a software sequence, partly on the FP64 pipe)
+    j0 = tile & ((1ll << logLR) - 1);
+    line0 = (tile >> logLR) << p.logC;
   }
 }
 
@@ -343,7 +349,7 @@ __device__ __forceinline__ void tile_compute_store(const PassParams& p, long lon
       tile_cr((long long)k * T, p.out_rcontig, logR, logC, ck, rk);
       if (ct + ck >= rem) continue;
       C v = F::from_s(sm[c * cs + pidx(r, sh)]);
-      if (p.do_scale) v = F::scale(v, p.scale);
+      if (p.do_scale) v = apply_scale<F>(v, p);
       gstore<F, OUT>(dst, p.out_off[k], v);
     }
     return;
@@ -358,7 +364,7 @@ __device__ __forceinline__ void tile_compute_store(const PassParams& p, long lon
     if (p.mode == 0) j += c; else line += c;
     if (line >= p.nlines) continue;
     C v = F::from_s(sm[c * cs + pidx(r, sh)]);
-    if (p.do_scale) v = F::scale(v, p.scale);
+    if (p.do_scale) v = apply_scale<F>(v, p);
     OE* base = reinterpret_cast<OE*>(p.out_ptrs[line]);
     const long long jd = ((j >> p.logNs) << (p.logNs + logR)) + (j & (p.Ns - 1));
     gstore<F, OUT>(base, (jd + ((long long)r << p.logNs)) * p.s, v);
@@ -594,7 +600,7 @@ __device__ __forceinline__ void last_subpass(const PassParams& p, long long line
 #pragma unroll
     for (int t = 0; t < Q; ++t) {
       C w = v[t];
-      if (p.do_scale) w = F::scale(w, p.scale);
+      if (p.do_scale) w = apply_scale<F>(w, p);
       gstore<F, OUT>(dst, t * step, w);
     }
   }
@@ -645,7 +651,7 @@ __device__ __forceinline__ void only_subpass(const PassParams& p, long long line
 #pragma unroll
     for (int t = 0; t < Q; ++t) {
       C w = v[t];
-      if (p.do_scale) w = F::scale(w, p.scale);
+      if (p.do_scale) w = apply_scale<F>(w, p);
       gstore<F, OUT>(dst, t * rs_out, w);
     }
   }
@@ -689,7 +695,9 @@ __device__ __forceinline__ void dft16_tc_products(const Dft16Frags& A, const flo
   for (int i = 0; i < 4; ++i) {
     split_tf32(xr[i], rh[i], rl[i]);
     split_tf32(xi[i], ih[i], il[i]);
-    split_tf32(-xi[i], nh[i], nl[i]);
+    // round-to-nearest-away is symmetric: the split of -x is the negated split of x
+    nh[i] = ih[i] ^ 0x80000000u;
+    nl[i] = il[i] ^ 0x80000000u;
   }
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
@@ -811,8 +819,8 @@ __device__ __forceinline__ void last_subpass16_tc(const PassParams& p, long long
       OE* dst = col_dst<OUT>(p, line0, j0, co) + jo * rs;
       F32::C y0 = {dr[c2], di[c2]}, y1 = {dr[2 + c2], di[2 + c2]};
       if (p.do_scale) {
-        y0 = F32::scale(y0, p.scale);
-        y1 = F32::scale(y1, p.scale);
+        y0 = apply_scale<F32>(y0, p);
+        y1 = apply_scale<F32>(y1, p);
       }
       gstore<F32, OUT>(dst, g * step, y0);
       gstore<F32, OUT>(dst, (g + 8) * step, y1);

@@ -71,6 +71,7 @@ struct PassParams {
   int q[4];         // log2 of the in-CTA sub-pass radices (sum = logR)
   int do_scale;
   double scale;
+  float fscale;     // scale as a float for the FP32-pipe forms (set at launch)
   long long tiles;  // grid size
   // Per-slot parts of the global element indices of a tile, for layouts
   // without per-line pointer tables: slot k of thread tid holds tile element
@@ -106,6 +107,10 @@ __host__ __device__ inline long long col_off_out(const PassParams& p, long long 
 }
 
 inline void set_slot_offsets(PassParams& p, int T) {
+  // the float copy of the output scale, converted once on the host so that no
+  // kernel converts it per element (a double->float conversion runs on the
+  // FP64 pipe)
+  p.fscale = (float)p.scale;
   const long long rs_in = (p.L >> p.logR) * p.s;
   const long long rs_out = p.Ns * p.s;
   for (int k = 0; k < kTileEPT; ++k) {

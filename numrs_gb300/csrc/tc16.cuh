@@ -123,7 +123,9 @@ __device__ __forceinline__ void subpass16_tc(f2* sm, int logR, int cs, int logNs
     for (int i = 0; i < 4; ++i) {
       split_tf32(xr[i], rh[i], rl[i]);
       split_tf32(xi[i], ih[i], il[i]);
-      split_tf32(-xi[i], nh[i], nl[i]);
+      // round-to-nearest-away is symmetric: the split of -x is the negated split of x
+      nh[i] = ih[i] ^ 0x80000000u;
+      nl[i] = il[i] ^ 0x80000000u;
     }
     float dr[4] = {0.f, 0.f, 0.f, 0.f}, di[4] = {0.f, 0.f, 0.f, 0.f};
     // Yr = Fr Xr + Fi (-Xi)
