@@ -19,7 +19,9 @@
  * stream) and synchronous unless opts->async is set.  Device arrays that a
  * transform works on in place must start on a 16-byte boundary (cudaMalloc
  * memory always does); an unaligned one is rejected with GBFFT_INVALID_ARG
- * before any launch.  Host arrays may start on any 8-byte boundary.  The
+ * before any launch.  Host arrays may start on any 8-byte boundary.  Calls
+ * share the library's work buffers: an asynchronous call on one stream is
+ * ordered (by an event) before any later call on another stream.  The
  * library is thread-safe (one internal lock).  No entry point changes any GPU
  * setting.
  */

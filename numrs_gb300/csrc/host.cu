@@ -41,6 +41,12 @@ struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;  // library stream
   cudaStream_t cur = nullptr;     // stream of the call in progress
+  // Calls share the library's work buffers.  An asynchronous device call
+  // records order_ev on its stream; a later call on another stream waits for
+  // it, so that calls never overlap on those buffers.
+  cudaEvent_t order_ev = nullptr;
+  cudaStream_t order_stream = nullptr;
+  bool order_pending = false;
   void* tw_dense[kForms] = {nullptr, nullptr, nullptr, nullptr};
   void* tw_part[kForms] = {nullptr, nullptr, nullptr, nullptr};
   DevBuf scratch;   // Stockham ping-pong buffer
@@ -122,6 +128,7 @@ int init_locked(int device) {
     return fail(GBFFT_CUDA_ERROR, "no CUDA device: %s", cudaGetErrorString(e));
   CK(cudaSetDevice(device));
   CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&g.order_ev, cudaEventDisableTiming));
   g.cur = g.stream;
   g.device = device;
   // On systems where the GPU reaches pageable host memory through the host's
@@ -524,9 +531,17 @@ int check_form(const Call& c) {
 struct StreamScope {
   explicit StreamScope(const Call& c) {
     g.cur = c.dev() ? (cudaStream_t)c.o->stream : g.stream;
+    if (g.order_pending && g.order_stream != g.cur) cudaStreamWaitEvent(g.cur, g.order_ev, 0);
   }
   int finish(const Call& c) {
-    if (!c.dev() || !c.o->async) CK(cudaStreamSynchronize(g.cur));
+    if (!c.dev() || !c.o->async) {
+      CK(cudaStreamSynchronize(g.cur));
+      g.order_pending = false;
+    } else {
+      CK(cudaEventRecord(g.order_ev, g.cur));
+      g.order_stream = g.cur;
+      g.order_pending = true;
+    }
     CK(cudaGetLastError());
     g.cur = g.stream;
     return GBFFT_OK;
@@ -891,9 +906,12 @@ int spectral_direct(Form f, int kind, const double* a, const double* b, long lon
 
 // Whether the plan of `nlines` lines of L points can run with host arrays read
 // and written by its first and last passes (at most two passes).
+// Whether run_axis_io can take the axis (at most two passes).
+bool io_fits(long long L, long long nlines, Form f) {
+  return L <= (1ll << kBatchMaxLog) && axis_plan(L, 1, nlines, 0, L, f).passes.size() <= 2;
+}
 bool direct_fits(long long L, long long nlines, Form f) {
-  return g.host_direct && L <= (1ll << kBatchMaxLog) &&
-         axis_plan(L, 1, nlines, 0, L, f).passes.size() <= 2;
+  return g.host_direct && io_fits(L, nlines, f);
 }
 
 }  // namespace
@@ -930,6 +948,7 @@ int gbfft_release(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g.inited) return GBFFT_OK;
   cudaDeviceSynchronize();
+  g.order_pending = false;
   for (DevBuf* b : {&g.scratch, &g.work, &g.stage_a, &g.stage_b, &g.stage_c, &g.ptrtab}) {
     if (b->p) cudaFree(b->p);
     b->p = nullptr;
@@ -1244,10 +1263,13 @@ static int spectral_call(const Call& c, int kind, const double* a, const double*
     else TRY(d2h(ans, w, n * sizeof(double)));
     return ss.finish(c);
   }
-  // the direct path moves the data (and correl's second input) and the answer
-  // as 16-byte vectors
-  if (!c.dev() && n >= 4 && al16(a) && al16(ans) && (kind != 2 || al16(b)) &&
-      direct_fits((long long)n / 2, 2, c.form()) && direct_fits((long long)n / 2, 1, c.form())) {
+  // Direct path: the first forward pass reads the caller's inputs through a
+  // pointer table and the last inverse pass writes the answer, with no copies
+  // (host arrays when the GPU reaches host memory, device arrays always).  It
+  // moves 16-byte vectors, so it needs aligned arrays.
+  if (n >= 4 && al16(a) && al16(ans) && (kind != 2 || al16(b)) &&
+      (c.dev() || g.host_direct) && io_fits((long long)n / 2, 2, c.form()) &&
+      io_fits((long long)n / 2, 1, c.form())) {
     TRY(spectral_direct(c.form(), kind, a, b, (long long)n, (long long)m, ans));
     return ss.finish(c);
   }

@@ -621,3 +621,29 @@ def test_autocorrel(nr, form, n):
         xd = torch.from_numpy(x).cuda()
         got = nr.autocorrel(xd).cpu().numpy()
         assert_fp64_close(got, ref, max(1, n.bit_length() - 1), "device autocorrel n=%d" % n)
+
+
+def test_async_calls_on_two_streams_are_ordered(nr):
+    """Asynchronous device calls on different streams share the library's work
+    buffers; the library orders each after the previous one, so back-to-back
+    convolutions on two streams both come out right."""
+    torch = pytest.importorskip("torch")
+    n = 1 << 16
+    xs = [W.normal(2000 + i, n) for i in range(4)]
+    r = W.normal(2100, 33)
+    refs = [O.convlv(x, r, 1)[1] for x in xs]
+    rd = torch.from_numpy(r).cuda()
+    xd = [torch.from_numpy(x).cuda() for x in xs]
+    outs = [torch.empty(n, dtype=torch.float64, device="cuda") for _ in xs]
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    torch.cuda.synchronize()
+    nr.set_async(True)
+    try:
+        for i in range(4):
+            with torch.cuda.stream(streams[i % 2]):
+                nr.convlv(xd[i], rd, 1, out=outs[i])
+    finally:
+        nr.set_async(False)
+    torch.cuda.synchronize()
+    for i in range(4):
+        assert_fp64_close(outs[i].cpu().numpy(), refs[i], 16, "two-stream convlv %d" % i)
