@@ -1,13 +1,18 @@
 // fft_core.cuh -- the Stockham pass kernel shared by every precision form.
 //
 // One launch performs one radix-R pass of a Stockham autosort FFT along an
-// axis (R <= 4096).  Each CTA loads a tile of C columns x R rows from global
-// memory (coalesced along whichever index is contiguous), multiplies by the
-// inter-pass twiddles, runs the R-point DFT of every column in shared memory
-// as a short sequence of radix-2/4/8/16 register sub-passes (themselves
-// Stockham steps), and stores the tile at the autosorted positions.  Axes of
+// axis (R <= 4096).  Each CTA owns a tile of C columns x R rows, multiplies by
+// the inter-pass twiddles, and runs the R-point DFT of every column as a short
+// sequence of radix-2/4/8/16 register sub-passes (themselves Stockham steps)
+// with shared memory between them.  Two tile schedules:
+//   staged  load the tile into shared memory, run the sub-passes there, store
+//           the tile (FP64, double-float)
+//   fused   the first sub-pass loads its butterfly inputs straight from global
+//           memory and the last one stores straight to global memory (FP32,
+//           TC32; every CUDA-core form in the persistent batch kernel)
+// Global accesses are coalesced along whichever index is contiguous.  Axes of
 // at most 4096 points take one launch; longer axes take 2-3 launches that
-// ping-pong through one scratch buffer, the last one in place.
+// ping-pong through scratch, the last one writing the caller's array.
 #pragma once
 #include "arith.cuh"
 #include "gbfft_internal.h"
