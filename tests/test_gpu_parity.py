@@ -647,3 +647,33 @@ def test_async_calls_on_two_streams_are_ordered(nr):
     torch.cuda.synchronize()
     for i in range(4):
         assert_fp64_close(outs[i].cpu().numpy(), refs[i], 16, "two-stream convlv %d" % i)
+
+
+def test_convlv_device_paths(nr):
+    """Device-array convolution and correlation: aligned arrays take the
+    copy-free path (inputs read through a pointer table), 8-byte-aligned views
+    and lengths beyond two passes take the copying path; all match the oracle."""
+    torch = pytest.importorskip("torch")
+    n = 1 << 14
+    x, y = W.normal(2200, n), W.normal(2201, n)
+    r = W.normal(2202, 65)
+    st, ref_c = O.convlv(x, r, 1)
+    st2, ref_r = O.correl(x, y)
+    for off in (0, 1):  # off = 1: views that start 8 bytes past a 16-byte boundary
+        bx = torch.zeros(n + 2, dtype=torch.float64, device="cuda")
+        by = torch.zeros(n + 2, dtype=torch.float64, device="cuda")
+        bo = torch.zeros(n + 2, dtype=torch.float64, device="cuda")
+        xv, yv, ov = bx[off:off + n], by[off:off + n], bo[off:off + n]
+        xv.copy_(torch.from_numpy(x))
+        yv.copy_(torch.from_numpy(y))
+        assert (xv.data_ptr() % 16 == 0) == (off == 0)
+        nr.convlv(xv, torch.from_numpy(r).cuda(), 1, out=ov)
+        assert_fp64_close(ov.cpu().numpy(), ref_c, 14, "device convlv off=%d" % off)
+        nr.correl(xv, yv, out=ov)
+        assert_fp64_close(ov.cpu().numpy(), ref_r, 14, "device correl off=%d" % off)
+    # 2^22 points: three passes per transform, beyond the copy-free path
+    big = 1 << 22
+    xb = W.normal(2203, big)
+    st, ref_b = O.convlv(xb, r, 1)
+    got = nr.convlv(torch.from_numpy(xb).cuda(), torch.from_numpy(r).cuda(), 1).cpu().numpy()
+    assert_fp64_close(got, ref_b, 22, "device convlv 2^22")
