@@ -151,11 +151,15 @@ def dist_setup():
 
 
 def max_over_ranks(x, world):
+    """Maximum of a per-rank scalar (timings) over the ranks: the job's time is
+    its slowest rank's.  Works on the NCCL (CUDA tensor) and gloo (CPU tensor)
+    backends."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
