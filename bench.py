@@ -425,6 +425,7 @@ def run_four1(args, world, rank, local):
     nn = 1 << log2n
     x = W.normal(W.BASE_SEED + 5, 2 * nn) if log2n <= 24 else None
     d = torch.from_numpy(x).to(dev) if x is not None else torch.randn(2 * nn, dtype=torch.float64, device=dev)
+    acc = _accuracy_vs_fp64(args.form, d, lambda t, form: nr.four1(t, nn, 1, form=form))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     nr.set_async(True)
     sign = [1]
@@ -482,8 +483,25 @@ def run_four1(args, world, rank, local):
         "compute_roofline": {"bound": "fp64" if args.form == "fp64" else "fp32",
                              "achieved_tflops": pass_flops / (pass_ms / 1e3) / 1e12 if pass_ms else 0.0,
                              "peak_tflops": FP64_PEAK_TFLOPS if args.form == "fp64" else 73.3},
-        "clocks": clk, "gpu_launches": launches,
+        "accuracy": acc, "clocks": clk, "gpu_launches": launches,
     }
+
+
+def _accuracy_vs_fp64(form, data, forward):
+    """rel-L2 of one forward transform in `form` against the same transform in
+    the FP64 form, on copies of `data` (the FP64 form itself is held to the CPU
+    oracle at 1e-12 by the parity tests).  For the FP64 form: None."""
+    if form == "fp64":
+        return None
+    import torch
+    ref = data.clone()
+    forward(ref, "fp64")
+    got = data.clone()
+    forward(got, form)
+    torch.cuda.synchronize()
+    e = float((got - ref).norm() / ref.norm())
+    del ref, got
+    return {"rel_l2_vs_fp64_form": e}
 
 
 def run_batch(args, world, rank, local):
@@ -714,6 +732,12 @@ def run_nd(args, world, rank, local):
             d.mul_(2.0 / n)
         flops = 2 * 2.5 * n * math.log2(n)
         wl = "rlft3 512^3 real f64 (1 GiB) + speq, forward + inverse (scaled 2/N) per step"
+    if args.workload == "fourn":
+        fwd = (lambda t, form: nr.fourn(t, shape, 3, 1, form=form))
+    else:
+        spw = torch.zeros_like(sp)
+        fwd = (lambda t, form: nr.rlft3(t, spw, 512, 512, 512, 1, form=form))
+    acc = _accuracy_vs_fp64(args.form, d, fwd) or {}
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
@@ -728,8 +752,9 @@ def run_nd(args, world, rank, local):
     nr.set_async(False)
     if rank != 0:
         return None
+    acc["roundtrip_rel_l2"] = err
     return _simple_line(args, world, wl, flops, total_ms, steps, launches, clk,
-                        {"roofline": roof, "accuracy": {"roundtrip_rel_l2": err}})
+                        {"roofline": roof, "accuracy": acc})
 
 
 def run_c1(args, world, rank, local):
