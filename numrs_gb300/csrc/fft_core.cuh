@@ -692,34 +692,6 @@ __device__ __forceinline__ void last_subpass_q(int lq, const PassParams& p, long
 // butterfly g of a chunk and, after the products, outputs k = g and g + 8 of
 // butterflies 2q and 2q + 1.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void dft16_tc_products(const Dft16Frags& A, const float (&xr)[4],
-                                                  const float (&xi)[4], float (&dr)[4],
-                                                  float (&di)[4]) {
-  uint32_t rh[4], rl[4], ih[4], il[4], nh[4], nl[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    split_tf32(xr[i], rh[i], rl[i]);
-    split_tf32(xi[i], ih[i], il[i]);
-    // round-to-nearest-away is symmetric: the split of -x is the negated split of x
-    nh[i] = ih[i] ^ 0x80000000u;
-    nl[i] = il[i] ^ 0x80000000u;
-  }
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    dr[r] = 0.f;
-    di[r] = 0.f;
-  }
-  // Yr = Fr Xr + Fi (-Xi);  Yi = Fi Xr + Fr Xi
-  mma3(dr, A.fr_hi[0], A.fr_lo[0], rh[0], rh[1], rl[0], rl[1]);
-  mma3(dr, A.fr_hi[1], A.fr_lo[1], rh[2], rh[3], rl[2], rl[3]);
-  mma3(dr, A.fi_hi[0], A.fi_lo[0], nh[0], nh[1], nl[0], nl[1]);
-  mma3(dr, A.fi_hi[1], A.fi_lo[1], nh[2], nh[3], nl[2], nl[3]);
-  mma3(di, A.fi_hi[0], A.fi_lo[0], rh[0], rh[1], rl[0], rl[1]);
-  mma3(di, A.fi_hi[1], A.fi_lo[1], rh[2], rh[3], rl[2], rl[3]);
-  mma3(di, A.fr_hi[0], A.fr_lo[0], ih[0], ih[1], il[0], il[1]);
-  mma3(di, A.fr_hi[1], A.fr_lo[1], ih[2], ih[3], il[2], il[3]);
-}
-
 // First radix-16 sub-pass from global memory (inter-pass twiddles applied on
 // the way in) to the shared tile.
 template <int SG, int IN, bool L2_ONLY>

@@ -77,6 +77,47 @@ __device__ __forceinline__ void mma3(float (&d)[4], const uint32_t (&ahi)[4],
   mma_tf32(d, ahi, bh0, bh1);
 }
 
+// The 16-point DFTs of 8 butterflies: lane (g, q) supplies inputs t = q + 4i
+// (i < 4) of butterfly g as xr/xi and receives outputs k = g, g + 8 of
+// butterflies 2q, 2q + 1 in dr/di (the C fragment layout).  Each output is the
+// FP32 sum of two product chains (Fr X and Fi X), each chain accumulated on
+// the tensor cores from zero: the tensor cores' accumulation rounding then
+// compounds over 6 products per chain instead of 12.
+__device__ __forceinline__ void dft16_tc_products(const Dft16Frags& A, const float (&xr)[4],
+                                                  const float (&xi)[4], float (&dr)[4],
+                                                  float (&di)[4]) {
+  // B fragments: k-block 0 holds t = q, q+4 (b0, b1); k-block 1 t = q+8, q+12
+  uint32_t rh[4], rl[4], ih[4], il[4], nh[4], nl[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    split_tf32(xr[i], rh[i], rl[i]);
+    split_tf32(xi[i], ih[i], il[i]);
+    // round-to-nearest-away is symmetric: the split of -x is the negated split of x
+    nh[i] = ih[i] ^ 0x80000000u;
+    nl[i] = il[i] ^ 0x80000000u;
+  }
+  float er[4] = {0.f, 0.f, 0.f, 0.f}, ei[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    dr[r] = 0.f;
+    di[r] = 0.f;
+  }
+  // Yr = Fr Xr + Fi (-Xi);  Yi = Fi Xr + Fr Xi
+  mma3(dr, A.fr_hi[0], A.fr_lo[0], rh[0], rh[1], rl[0], rl[1]);
+  mma3(dr, A.fr_hi[1], A.fr_lo[1], rh[2], rh[3], rl[2], rl[3]);
+  mma3(er, A.fi_hi[0], A.fi_lo[0], nh[0], nh[1], nl[0], nl[1]);
+  mma3(er, A.fi_hi[1], A.fi_lo[1], nh[2], nh[3], nl[2], nl[3]);
+  mma3(di, A.fi_hi[0], A.fi_lo[0], rh[0], rh[1], rl[0], rl[1]);
+  mma3(di, A.fi_hi[1], A.fi_lo[1], rh[2], rh[3], rl[2], rl[3]);
+  mma3(ei, A.fr_hi[0], A.fr_lo[0], ih[0], ih[1], il[0], il[1]);
+  mma3(ei, A.fr_hi[1], A.fr_lo[1], ih[2], ih[3], il[2], il[3]);
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    dr[r] += er[r];
+    di[r] += ei[r];
+  }
+}
+
 // One radix-16 Stockham sub-pass over C columns of R points in shared memory
 // (layout and index rules as subpass<F, SG, 16> in fft_core.cuh).  Each warp
 // takes 32 consecutive butterflies in four chunks of 8 (the mma N dimension).
@@ -117,27 +158,8 @@ __device__ __forceinline__ void subpass16_tc(f2* sm, int logR, int cs, int logNs
       xr[i] = v.x;
       xi[i] = v.y;
     }
-    // B fragments: k-block 0 holds t = q, q+4 (b0, b1); k-block 1 t = q+8, q+12
-    uint32_t rh[4], rl[4], ih[4], il[4], nh[4], nl[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      split_tf32(xr[i], rh[i], rl[i]);
-      split_tf32(xi[i], ih[i], il[i]);
-      // round-to-nearest-away is symmetric: the split of -x is the negated split of x
-      nh[i] = ih[i] ^ 0x80000000u;
-      nl[i] = il[i] ^ 0x80000000u;
-    }
-    float dr[4] = {0.f, 0.f, 0.f, 0.f}, di[4] = {0.f, 0.f, 0.f, 0.f};
-    // Yr = Fr Xr + Fi (-Xi)
-    mma3(dr, A.fr_hi[0], A.fr_lo[0], rh[0], rh[1], rl[0], rl[1]);
-    mma3(dr, A.fr_hi[1], A.fr_lo[1], rh[2], rh[3], rl[2], rl[3]);
-    mma3(dr, A.fi_hi[0], A.fi_lo[0], nh[0], nh[1], nl[0], nl[1]);
-    mma3(dr, A.fi_hi[1], A.fi_lo[1], nh[2], nh[3], nl[2], nl[3]);
-    // Yi = Fi Xr + Fr Xi
-    mma3(di, A.fi_hi[0], A.fi_lo[0], rh[0], rh[1], rl[0], rl[1]);
-    mma3(di, A.fi_hi[1], A.fi_lo[1], rh[2], rh[3], rl[2], rl[3]);
-    mma3(di, A.fr_hi[0], A.fr_lo[0], ih[0], ih[1], il[0], il[1]);
-    mma3(di, A.fr_hi[1], A.fr_lo[1], ih[2], ih[3], il[2], il[3]);
+    float dr[4], di[4];
+    dft16_tc_products(A, xr, xi, dr, di);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       yr[ch][r] = dr[r];
