@@ -80,9 +80,11 @@ __device__ __forceinline__ void mma3(float (&d)[4], const uint32_t (&ahi)[4],
 // The 16-point DFTs of 8 butterflies: lane (g, q) supplies inputs t = q + 4i
 // (i < 4) of butterfly g as xr/xi and receives outputs k = g, g + 8 of
 // butterflies 2q, 2q + 1 in dr/di (the C fragment layout).  Each output is the
-// FP32 sum of two product chains (Fr X and Fi X), each chain accumulated on
-// the tensor cores from zero: the tensor cores' accumulation rounding then
-// compounds over 6 products per chain instead of 12.
+// FP32 (round-to-nearest) sum of four product chains, one per matrix (Fr, Fi)
+// and k-block, each accumulated on the tensor cores from zero.  The tensor
+// cores' accumulation rounding, which is not round-to-nearest, then compounds
+// over 3 products per chain instead of 12: measured, this cuts the form's
+// error about 3x.
 __device__ __forceinline__ void dft16_tc_products(const Dft16Frags& A, const float (&xr)[4],
                                                   const float (&xi)[4], float (&dr)[4],
                                                   float (&di)[4]) {
@@ -96,25 +98,24 @@ __device__ __forceinline__ void dft16_tc_products(const Dft16Frags& A, const flo
     nh[i] = ih[i] ^ 0x80000000u;
     nl[i] = il[i] ^ 0x80000000u;
   }
-  float er[4] = {0.f, 0.f, 0.f, 0.f}, ei[4] = {0.f, 0.f, 0.f, 0.f};
+  float c[8][4];
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) c[k][r] = 0.f;
+  // Yr = Fr Xr + Fi (-Xi);  Yi = Fi Xr + Fr Xi; one chain per matrix and k-block
+  mma3(c[0], A.fr_hi[0], A.fr_lo[0], rh[0], rh[1], rl[0], rl[1]);
+  mma3(c[1], A.fr_hi[1], A.fr_lo[1], rh[2], rh[3], rl[2], rl[3]);
+  mma3(c[2], A.fi_hi[0], A.fi_lo[0], nh[0], nh[1], nl[0], nl[1]);
+  mma3(c[3], A.fi_hi[1], A.fi_lo[1], nh[2], nh[3], nl[2], nl[3]);
+  mma3(c[4], A.fi_hi[0], A.fi_lo[0], rh[0], rh[1], rl[0], rl[1]);
+  mma3(c[5], A.fi_hi[1], A.fi_lo[1], rh[2], rh[3], rl[2], rl[3]);
+  mma3(c[6], A.fr_hi[0], A.fr_lo[0], ih[0], ih[1], il[0], il[1]);
+  mma3(c[7], A.fr_hi[1], A.fr_lo[1], ih[2], ih[3], il[2], il[3]);
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
-    dr[r] = 0.f;
-    di[r] = 0.f;
-  }
-  // Yr = Fr Xr + Fi (-Xi);  Yi = Fi Xr + Fr Xi
-  mma3(dr, A.fr_hi[0], A.fr_lo[0], rh[0], rh[1], rl[0], rl[1]);
-  mma3(dr, A.fr_hi[1], A.fr_lo[1], rh[2], rh[3], rl[2], rl[3]);
-  mma3(er, A.fi_hi[0], A.fi_lo[0], nh[0], nh[1], nl[0], nl[1]);
-  mma3(er, A.fi_hi[1], A.fi_lo[1], nh[2], nh[3], nl[2], nl[3]);
-  mma3(di, A.fi_hi[0], A.fi_lo[0], rh[0], rh[1], rl[0], rl[1]);
-  mma3(di, A.fi_hi[1], A.fi_lo[1], rh[2], rh[3], rl[2], rl[3]);
-  mma3(ei, A.fr_hi[0], A.fr_lo[0], ih[0], ih[1], il[0], il[1]);
-  mma3(ei, A.fr_hi[1], A.fr_lo[1], ih[2], ih[3], il[2], il[3]);
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    dr[r] += er[r];
-    di[r] += ei[r];
+    dr[r] = (c[0][r] + c[1][r]) + (c[2][r] + c[3][r]);
+    di[r] = (c[4][r] + c[5][r]) + (c[6][r] + c[7][r]);
   }
 }
 
