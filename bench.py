@@ -19,8 +19,8 @@ is 3 real FFTs per call, 2.5 N log2 N flops each.
 
 --impl reference times the CPU oracle alone (the reference crate itself
 cannot be built: no Rust toolchain, and its FFT modules are not compiled).
-Other workloads (--workload four1|batch|fourn|rlft3|large) exercise the other
-configurations; the driver runs the default.
+Other workloads (--workload four1|large|batch|fourn|rlft3|c1|convbatch) exercise the other
+configurations; with no flags the convolution/correlation workload runs.
 """
 import argparse
 import json
@@ -38,7 +38,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "FFT GFLOP/s (5N·log2N) & HBM GB/s vs peak; TC-split vs FP64 at rel-L2≤1e-6"
-FP64_PEAK_TFLOPS = 1.20  # DFMA loop measured on this machine's GB300 (probe recorded in the design doc)
+FP64_PEAK_TFLOPS = 1.20  # DFMA-loop throughput measured on GB300 (2 DFMA lanes per SM per cycle)
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
 # capture of the same workload (dram__bytes_read.sum + dram__bytes_write.sum),
