@@ -1,354 +1,43 @@
-// batch.cu -- persistent batched FFT over thousands of transforms of uneven
-// power-of-two sizes in one launch (FFTProcessor::fft_batch,
-// src/FFT_1.rs:185-190, which runs one rayon task per transform).
-//
-// The host sorts the transforms into size bins and lays the work out as a
-// queue of tiles:
-//
-//   [pass 1 of every two-pass bin] [single-pass bins, largest first]
-//   [pass 2 of every two-pass bin]
-//
-// Resident CTAs take tiles from the queue with one atomicAdd each.  A pass-2
-// tile needs every pass-1 tile of its transform: pass-1 tiles bump a
-// per-transform counter after a fence, and a pass-2 tile polls that counter.
-// The poll is bounded (spin_limit iterations with __nanosleep); if it runs out
-// the CTA records an error flag, skips the tile and goes on, and the host
-// reports GBFFT_TIMEOUT.  A pass-2 tile only ever waits on tiles that were
-// handed out before it, so the wait always ends unless a CTA died.
-#include "fft_core.cuh"
+// batch.cu -- form dispatch of the persistent batched-FFT launchers.  The
+// kernels of each form live in their own translation unit (batch_<form>.cu).
 #include "batch.h"
-#include "tma.cuh"
 
 namespace gbfft {
 
-template <class F, int SG, int SIO>
-__global__ void __launch_bounds__(256, (F::kind == 1 && !F::kTensor ? 3 : 2))
-    k_batch(BatchParams P) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  typename F::S* sm = reinterpret_cast<typename F::S*>(smem_raw);
-  __shared__ long long s_item;
-  __shared__ int s_ok;
-  const int tid = threadIdx.x;
-  for (;;) {
-    if (tid == 0) s_item = (long long)atomicAdd(P.head, 1ull);
-    __syncthreads();
-    const long long item = s_item;
-    __syncthreads();
-    if (item >= P.total) break;
-    int ri = 0;
-    while (ri + 1 < P.nranges && item >= P.ranges[ri + 1].item0) ++ri;
-    const BatchRange& R = P.ranges[ri];
-    const PassParams& p = R.p;
-    const long long tile = item - R.item0;
-    // mode-0 tiles of the two-pass bins cover one transform each
-    const long long line0 = (R.kind != 0) ? (tile >> ((p.logL - p.logR) - p.logC)) : 0;
-    if (R.kind == 2) {
-      if (tid == 0) {
-        volatile unsigned int* cnt = P.done + R.first + line0;
-        unsigned int it = 0;
-        int ok = 1;
-        while (*cnt < R.need) {
-          if (++it > P.spin_limit) {
-            atomicExch(P.err, 1);
-            ok = 0;
-            break;
-          }
-          __nanosleep(128);
-        }
-        __threadfence();
-        s_ok = ok;
-      }
-      __syncthreads();
-      if (!s_ok) continue;
-      run_tile<F, SG, SIO, IO_D2, 256, true, true>(p, tile, sm, tid);
-    } else if (R.kind == 1) {
-      run_tile<F, SG, IO_D2, SIO, 256, false, true>(p, tile, sm, tid);
-      __threadfence();
-      __syncthreads();
-      if (tid == 0) atomicAdd(P.done + R.first + line0, 1u);
-    } else {
-      run_tile<F, SG, IO_D2, IO_D2, 256, false, true>(p, tile, sm, tid);
-    }
-    __syncthreads();
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Prefetching variant (FP32, tensor-core and double-float forms, all caller
-// arrays 16-byte aligned).  While a CTA computes one tile, warp 0 has the
-// bulk-copy engine (cp.async.bulk, completed on an mbarrier) bring the raw
-// elements of the CTA's next tile into a staging buffer, so the load latency
-// of one tile hides behind the arithmetic of the previous one.  Pass-2 tiles
-// of two-pass bins are not prefetched: they must first see their transform's
-// pass-1 counter, so they load as in k_batch.
-// Shared memory: [staging: 4096 x 16 B][padded tile][mbarrier]
-// ---------------------------------------------------------------------------
-constexpr size_t kStagingBytes = size_t(kEPT) * 256 * 16;
-// try_wait calls before a bulk-copy wait gives up (each may suspend the
-// thread for a short hardware-defined time)
-constexpr uint32_t kCopyWaitLimit = 1u << 20;
-
-// Warp 0: start the bulk copies of `item` into staging.  Returns 1 when copies
-// were issued (the mbarrier will complete a phase), 0 when nothing was (end
-// of queue or a pass-2 tile).
-__device__ __forceinline__ int prefetch_item(const BatchParams& P, long long item, d2* staging,
-                                             uint64_t* bar, int lane) {
-  if (item >= P.total) return 0;
-  int ri = 0;
-  while (ri + 1 < P.nranges && item >= P.ranges[ri + 1].item0) ++ri;
-  const BatchRange& R = P.ranges[ri];
-  if (R.kind == 2) return 0;
-  const PassParams& p = R.p;
-  long long line0, j0;
-  tile_origin(p, item - R.item0, line0, j0);
-  const int Rn = 1 << p.logR, Cn = 1 << p.logC;
-  int ncopies;
-  uint32_t bytes_each;
-  if (p.in_rcontig) {
-    // single-pass bin: one contiguous transform per column
-    long long valid = p.nlines - line0;
-    ncopies = (int)(valid < Cn ? valid : Cn);
-    bytes_each = (uint32_t)Rn * 16u;
-  } else {
-    // pass 1 of a two-pass bin: one run of C elements per row
-    ncopies = Rn;
-    bytes_each = (uint32_t)Cn * 16u;
-  }
-  if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)ncopies * bytes_each);
-  __syncwarp();
-  for (int i = lane; i < ncopies; i += 32) {
-    const d2* src;
-    d2* dst;
-    if (p.in_rcontig) {
-      src = reinterpret_cast<const d2*>(p.in_ptrs[line0 + i]);
-      dst = staging + (size_t)i * Rn;
-    } else {
-      src = reinterpret_cast<const d2*>(p.in_ptrs[line0]) + j0 +
-            ((long long)i << (p.logL - p.logR));
-      dst = staging + (size_t)i * Cn;
-    }
-    bulk_copy_g2s(dst, src, bytes_each, bar);
-  }
-  return 1;
-}
-
-template <class F, int SG, int SIO>
-__global__ void __launch_bounds__(256, (F::kind == 2 ? 1 : 2)) k_batch_pf(BatchParams P) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  d2* staging = reinterpret_cast<d2*>(smem_raw);
-  typename F::S* sm = reinterpret_cast<typename F::S*>(smem_raw + kStagingBytes);
-  __shared__ __align__(8) uint64_t bar;
-  __shared__ long long s_item, s_next;
-  __shared__ int s_pref, s_pref_next, s_ok, s_fail;
-  const int tid = threadIdx.x, lane = tid & 31;
-  if (tid == 0) {
-    mbar_init(&bar, 1);
-    fence_mbar_init();
-    s_fail = 0;
-  }
-  __syncthreads();
-  if (tid < 32) {
-    long long it = 0;
-    if (lane == 0) it = (long long)atomicAdd(P.head, 1ull);
-    it = __shfl_sync(0xffffffffu, it, 0);
-    const int pf = prefetch_item(P, it, staging, &bar, lane);
-    if (lane == 0) {
-      s_item = it;
-      s_pref = pf;
-    }
-  }
-  __syncthreads();
-  uint32_t parity = 0;
-  for (;;) {
-    const long long item = s_item;
-    const int pref = s_pref;
-    if (item >= P.total) break;
-    int ri = 0;
-    while (ri + 1 < P.nranges && item >= P.ranges[ri + 1].item0) ++ri;
-    const BatchRange& R = P.ranges[ri];
-    const PassParams& p = R.p;
-    const long long tile = item - R.item0;
-    long long line0, j0;
-    tile_origin(p, tile, line0, j0);
-    if (pref) {
-      // every thread waits for the bulk copies (bounded), then stages its
-      // sixteen elements from the staging buffer into the padded tile
-      if (!mbar_wait_bounded(&bar, parity, kCopyWaitLimit)) atomicOr(&s_fail, 1);
-      parity ^= 1u;
-      __syncthreads();
-      if (s_fail) {
-        if (tid == 0) atomicExch(P.err, 1);
-        break;
-      }
-#pragma unroll
-      for (int k = 0; k < kEPT; ++k) {
-        const int e = tid + k * 256;
-        stage_elem<F, SG, IO_D2>(p, line0, j0, e, staging[e], sm);
-      }
-    } else {
-      // pass-2 tile: wait for the transform's pass-1 tiles, then load
-      if (tid == 0) {
-        volatile unsigned int* cnt = P.done + R.first + line0;
-        unsigned int it = 0;
-        int ok = 1;
-        while (*cnt < R.need) {
-          if (++it > P.spin_limit) {
-            atomicExch(P.err, 1);
-            ok = 0;
-            break;
-          }
-          __nanosleep(128);
-        }
-        __threadfence();
-        s_ok = ok;
-      }
-      __syncthreads();
-      if (!s_ok) break;  // error already recorded; the host reports GBFFT_TIMEOUT
-      using IE = typename IOElem<SIO>::T;
-      IE raw[kEPT];
-      load_tile_raw<IE, SIO, 256, true>(p, line0, j0, tid, raw);
-#pragma unroll
-      for (int k = 0; k < kEPT; ++k) stage_elem<F, SG, SIO>(p, line0, j0, tid + k * 256, raw[k], sm);
-    }
-    __syncthreads();  // tile staged; the staging buffer is free again
-    if (tid < 32) {
-      fence_proxy_async_smem();
-      long long nx = 0;
-      if (lane == 0) nx = (long long)atomicAdd(P.head, 1ull);
-      nx = __shfl_sync(0xffffffffu, nx, 0);
-      const int pf = prefetch_item(P, nx, staging, &bar, lane);
-      if (lane == 0) {
-        s_next = nx;
-        s_pref_next = pf;
-      }
-    }
-    if (R.kind == 1) {
-      tile_compute_store<F, SG, SIO, 256>(p, line0, j0, sm, tid);
-      __threadfence();
-      __syncthreads();
-      if (tid == 0) atomicAdd(P.done + R.first + line0, 1u);
-    } else {
-      tile_compute_store<F, SG, IO_D2, 256>(p, line0, j0, sm, tid);
-    }
-    __syncthreads();
-    if (tid == 0) {
-      s_item = s_next;
-      s_pref = s_pref_next;
-    }
-    __syncthreads();
-  }
-  // a copy still in flight (only after a failed wait) must land before exit
-  if (s_pref && s_item < P.total) mbar_wait_bounded(&bar, parity, kCopyWaitLimit);
-}
-
-template <class F>
-inline size_t pf_smem_bytes() {
-  return kStagingBytes + pass_smem_bytes<F>(256);
-}
-
-template <class F, int SG, int SIO>
-static cudaError_t prepare_pf_t() {
-  static bool done = false;
-  if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(k_batch_pf<F, SG, SIO>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)pf_smem_bytes<F>());
-  if (e == cudaSuccess) done = true;
-  return e;
-}
-
-template <class F, int SG, int SIO>
-static cudaError_t launch_batch_pf_t(const BatchParams& P, int grid, cudaStream_t st) {
-  cudaError_t e = prepare_pf_t<F, SG, SIO>();
-  if (e != cudaSuccess) return e;
-  k_batch_pf<F, SG, SIO><<<grid, 256, pf_smem_bytes<F>(), st>>>(P);
-  return cudaGetLastError();
-}
-
-template <class F, int SG, int SIO>
-static int occupancy_pf_t() {
-  int n = 0;
-  if (prepare_pf_t<F, SG, SIO>() != cudaSuccess) return 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_pf<F, SG, SIO>, 256,
-                                                pf_smem_bytes<F>());
-  return n;
-}
-
-// Raise the dynamic shared memory limit of one instantiation (idempotent;
-// called before any stream capture).
-template <class F, int SG, int SIO>
-static cudaError_t prepare_t() {
-  static bool done = false;
-  if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(k_batch<F, SG, SIO>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)pass_smem_bytes<F>(256));
-  if (e == cudaSuccess) done = true;
-  return e;
-}
-
-template <class F, int SG, int SIO>
-static cudaError_t launch_batch_t(const BatchParams& P, int grid, cudaStream_t st) {
-  cudaError_t e = prepare_t<F, SG, SIO>();
-  if (e != cudaSuccess) return e;
-  k_batch<F, SG, SIO><<<grid, 256, pass_smem_bytes<F>(256), st>>>(P);
-  return cudaGetLastError();
-}
-
-template <class F, int SG, int SIO>
-static int occupancy_t() {
-  int n = 0;
-  if (prepare_t<F, SG, SIO>() != cudaSuccess) return 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<F, SG, SIO>, 256,
-                                                pass_smem_bytes<F>(256));
-  return n;
-}
-
-cudaError_t launch_batch_pf(Form f, int sign, const BatchParams& P, int grid, cudaStream_t st) {
-  if (f == FORM_F32)
-    return sign > 0 ? launch_batch_pf_t<F32, 1, IO_F2>(P, grid, st)
-                    : launch_batch_pf_t<F32, -1, IO_F2>(P, grid, st);
-  if (f == FORM_TC32)
-    return sign > 0 ? launch_batch_pf_t<TC32, 1, IO_F2>(P, grid, st)
-                    : launch_batch_pf_t<TC32, -1, IO_F2>(P, grid, st);
-  if (f == FORM_DF64)
-    return sign > 0 ? launch_batch_pf_t<DF64, 1, IO_F4>(P, grid, st)
-                    : launch_batch_pf_t<DF64, -1, IO_F4>(P, grid, st);
-  return cudaErrorInvalidValue;
-}
-
-int batch_pf_blocks_per_sm(Form f, int sign) {
-  if (f == FORM_F32)
-    return sign > 0 ? occupancy_pf_t<F32, 1, IO_F2>() : occupancy_pf_t<F32, -1, IO_F2>();
-  if (f == FORM_TC32)
-    return sign > 0 ? occupancy_pf_t<TC32, 1, IO_F2>() : occupancy_pf_t<TC32, -1, IO_F2>();
-  if (f == FORM_DF64)
-    return sign > 0 ? occupancy_pf_t<DF64, 1, IO_F4>() : occupancy_pf_t<DF64, -1, IO_F4>();
-  return 0;
-}
-
 cudaError_t launch_batch(Form f, int sign, const BatchParams& P, int grid, cudaStream_t st) {
-  if (f == FORM_F64)
-    return sign > 0 ? launch_batch_t<F64, 1, IO_D2>(P, grid, st)
-                    : launch_batch_t<F64, -1, IO_D2>(P, grid, st);
-  if (f == FORM_F32)
-    return sign > 0 ? launch_batch_t<F32, 1, IO_F2>(P, grid, st)
-                    : launch_batch_t<F32, -1, IO_F2>(P, grid, st);
-  if (f == FORM_TC32)
-    return sign > 0 ? launch_batch_t<TC32, 1, IO_F2>(P, grid, st)
-                    : launch_batch_t<TC32, -1, IO_F2>(P, grid, st);
-  return sign > 0 ? launch_batch_t<DF64, 1, IO_F4>(P, grid, st)
-                  : launch_batch_t<DF64, -1, IO_F4>(P, grid, st);
+  switch (f) {
+    case FORM_F64: return launch_batch_f64(sign, P, grid, st);
+    case FORM_F32: return launch_batch_f32(sign, P, grid, st);
+    case FORM_TC32: return launch_batch_tc32(sign, P, grid, st);
+    default: return launch_batch_df64(sign, P, grid, st);
+  }
 }
 
 int batch_blocks_per_sm(Form f, int sign) {
-  if (f == FORM_F64)
-    return sign > 0 ? occupancy_t<F64, 1, IO_D2>() : occupancy_t<F64, -1, IO_D2>();
-  if (f == FORM_F32)
-    return sign > 0 ? occupancy_t<F32, 1, IO_F2>() : occupancy_t<F32, -1, IO_F2>();
-  if (f == FORM_TC32)
-    return sign > 0 ? occupancy_t<TC32, 1, IO_F2>() : occupancy_t<TC32, -1, IO_F2>();
-  return sign > 0 ? occupancy_t<DF64, 1, IO_F4>() : occupancy_t<DF64, -1, IO_F4>();
+  switch (f) {
+    case FORM_F64: return batch_blocks_per_sm_f64(sign);
+    case FORM_F32: return batch_blocks_per_sm_f32(sign);
+    case FORM_TC32: return batch_blocks_per_sm_tc32(sign);
+    default: return batch_blocks_per_sm_df64(sign);
+  }
+}
+
+cudaError_t launch_batch_pf(Form f, int sign, const BatchParams& P, int grid, cudaStream_t st) {
+  switch (f) {
+    case FORM_F32: return launch_batch_pf_f32(sign, P, grid, st);
+    case FORM_TC32: return launch_batch_pf_tc32(sign, P, grid, st);
+    case FORM_DF64: return launch_batch_pf_df64(sign, P, grid, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+int batch_pf_blocks_per_sm(Form f, int sign) {
+  switch (f) {
+    case FORM_F32: return batch_pf_blocks_per_sm_f32(sign);
+    case FORM_TC32: return batch_pf_blocks_per_sm_tc32(sign);
+    case FORM_DF64: return batch_pf_blocks_per_sm_df64(sign);
+    default: return 0;
+  }
 }
 
 }  // namespace gbfft

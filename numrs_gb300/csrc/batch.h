@@ -45,4 +45,20 @@ int batch_blocks_per_sm(Form f, int sign);
 cudaError_t launch_batch_pf(Form f, int sign, const BatchParams& P, int grid, cudaStream_t st);
 int batch_pf_blocks_per_sm(Form f, int sign);
 
+// per-form launchers (batch_<form>.cu), behind the dispatchers above
+cudaError_t launch_batch_f64(int sign, const BatchParams& P, int grid, cudaStream_t st);
+cudaError_t launch_batch_f32(int sign, const BatchParams& P, int grid, cudaStream_t st);
+cudaError_t launch_batch_tc32(int sign, const BatchParams& P, int grid, cudaStream_t st);
+cudaError_t launch_batch_df64(int sign, const BatchParams& P, int grid, cudaStream_t st);
+int batch_blocks_per_sm_f64(int sign);
+int batch_blocks_per_sm_f32(int sign);
+int batch_blocks_per_sm_tc32(int sign);
+int batch_blocks_per_sm_df64(int sign);
+cudaError_t launch_batch_pf_f32(int sign, const BatchParams& P, int grid, cudaStream_t st);
+cudaError_t launch_batch_pf_tc32(int sign, const BatchParams& P, int grid, cudaStream_t st);
+cudaError_t launch_batch_pf_df64(int sign, const BatchParams& P, int grid, cudaStream_t st);
+int batch_pf_blocks_per_sm_f32(int sign);
+int batch_pf_blocks_per_sm_tc32(int sign);
+int batch_pf_blocks_per_sm_df64(int sign);
+
 }  // namespace gbfft

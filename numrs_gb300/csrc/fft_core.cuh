@@ -359,7 +359,6 @@ __device__ __forceinline__ void tile_compute_store(const PassParams& p, long lon
     }
     return;
   }
-  const long long lqmask = (1ll << p.lq_log) - 1;
 #pragma unroll 4
   for (int k = 0; k < kEPT; ++k) {
     const int e = tid + k * T;
