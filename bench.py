@@ -1,26 +1,33 @@
 #!/usr/bin/env python3
 """Benchmark of the FFT family on GB300 (one JSON line on stdout).
 
-Default workload: realft-based convolution and correlation of an N = 2^20
-real f64 signal (i.i.d. N(0,1)) with a 257-tap response (Gaussian window,
-sigma = m/6, times N(0,1)) stored in wrap-around order in a length-N buffer.
-One step = one convlv(isign=+1) call and one correl call.  The nominal work
-is 3 real FFTs per call, 2.5 N log2 N flops each.
+Default workload (the largest configuration that runs on one GPU): one
+complex four1 of nn = 2^28 points (4 GiB of interleaved f64), i.i.d. N(0,1)
+from the seeded generator, FP64 arithmetic.  One step = one in-place forward
+transform; the nominal work is 5 nn log2 nn flops.
 
-  value     GFLOP/s with inputs resident in HBM (device tensors through the
-            C ABI), CUDA events on the launching stream, L2 flushed (256 MiB
-            write) before every timed step
-  e2e       the same steps through the C ABI with pinned host buffers, the
-            host->device and device->host copies inside the timed region
-  roofline  the Stockham pass kernel: algorithmic bytes / its event-timed
-            duration against the measured HBM copy bandwidth
-  cpu_baseline  the CPU oracle (a C++ restatement of the crate's routines)
-            on the host cores for a bounded sample of the same workload
+  value     GFLOP/s with the input resident in HBM (device tensor through the
+            C ABI), CUDA events on the launching stream around each transform;
+            the input is restored from a device copy between steps, outside
+            the events.  The 4 GiB input is larger than L2.
+  e2e       the same transform through the C ABI on a pinned host array: the
+            host->device copy, the transform and the device->host copy are
+            inside each timed call
+  roofline  the Stockham pass kernel: algorithmic bytes per launch over its
+            event-timed duration, against the measured HBM copy bandwidth;
+            compute_roofline gives the same kernel against the FP64 pipe
+  forms     the double-float, FP32 and tensor-core forms on the same step,
+            with their rel-L2 against the FP64 form
+  batch_target  the batched configuration (20,000 transforms of 2^6..2^14
+            points, amplitudes 10^u): transforms/s of every form and the
+            tensor-core form's per-transform rel-L2 against FP64
+  cpu_baseline  the CPU oracle (a C++ restatement of the crate's routines) on
+            the host cores, on a bounded sample of the workload
 
---impl reference times the CPU oracle alone (the reference crate itself
-cannot be built: no Rust toolchain, and its FFT modules are not compiled).
-Other workloads (--workload four1|large|batch|fourn|rlft3|c1|convbatch) exercise the other
-configurations; with no flags the convolution/correlation workload runs.
+--impl reference times the CPU oracle alone on the same configuration (the
+crate itself cannot be built: no Rust toolchain, and its FFT modules are not
+compiled).  Other workloads (--workload convlv|four1|batch|fourn|rlft3|c1|convbatch)
+exercise the other configurations.
 """
 import argparse
 import json
@@ -29,7 +36,6 @@ import os
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -39,38 +45,42 @@ sys.path.insert(0, ROOT)
 
 METRIC = "FFT GFLOP/s (5N·log2N) & HBM GB/s vs peak; TC-split vs FP64 at rel-L2≤1e-6"
 FP64_PEAK_TFLOPS = 1.20  # DFMA-loop throughput measured on GB300 (2 DFMA lanes per SM per cycle)
+FP32_PEAK_TFLOPS = 73.3  # FFMA-loop throughput measured on GB300
 
-# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
-# capture of the same workload (dram__bytes_read.sum + dram__bytes_write.sum),
-# keyed by (workload, form).  The summaries under profiles/ give the commands.
-MEASURED_TRAFFIC = {
-    # 40 k_pass launches of the device-resident steps: forward 16.93 MB, inverse 8.54 MB
-    ("convlv", "fp64"): (12.74e6, "profiles/k_pass_f64_convlv_correl_n2p20.md"),
-    # the three passes of one 2^24-point transform: 367.1, 218.5, 346.0 MB
-    ("four1_24", "fp32"): (310.5e6, "profiles/k_pass_fp32_fused_four1_n2p24.md"),
-    # one persistent launch over the 20,000 transforms
-    ("batch", "fp32"): (3.2058e9, "profiles/k_batch_c3_20000_transforms.md"),
-    ("batch", "tc32"): (3.2069e9, "profiles/k_batch_c3_20000_transforms.md"),
+LARGE_LOG2N = 28
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# dominant kernel from one ncu capture of the same kernel on the same
+# workload, keyed by (workload, form).  Fixed numbers from an earlier capture,
+# not measured by this run.
+NCU_TRAFFIC = {
+    ("convlv", "fp64"): 12.74e6,
+    ("four1_24", "fp32"): 310.5e6,
+    ("batch", "fp32"): 3.2058e9,
+    ("batch", "tc32"): 3.2069e9,
 }
 
 
 def traffic_of(workload, form):
-    t = MEASURED_TRAFFIC.get((workload, form))
-    return (t[0], t[1]) if t else (None, None)
+    t = NCU_TRAFFIC.get((workload, form))
+    if t is None:
+        return None, None
+    return t, "ncu capture of this kernel and workload (fixed, not measured in this run)"
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="convlv",
-                    choices=["convlv", "four1", "batch", "fourn", "rlft3", "large", "c1", "convbatch"])
+    ap.add_argument("--workload", default="large",
+                    choices=["large", "convlv", "four1", "batch", "fourn", "rlft3", "c1", "convbatch"])
     ap.add_argument("--form", default="fp64", choices=["fp64", "df64", "fp32", "tc32"])
     ap.add_argument("--no-forms", action="store_true", help="skip the extra precision forms")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched target in the default line")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--log2n", type=int, default=0, help="four1 workload size (default 2^24)")
+    ap.add_argument("--log2n", type=int, default=0, help="four1 workload size (default 2^24; large: 2^28)")
     return ap.parse_args()
 
 
@@ -82,6 +92,10 @@ def peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def host_cores():
+    return os.cpu_count() or 1
 
 
 # ---------------------------------------------------------------------------
@@ -141,7 +155,7 @@ class Clocks:
 
 
 # ---------------------------------------------------------------------------
-# distributed bookkeeping (one process per GPU; replicas of the workload)
+# distributed bookkeeping (one process per GPU)
 # ---------------------------------------------------------------------------
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -170,8 +184,360 @@ def barrier(world):
         dist.barrier()
 
 
+def _events(n):
+    import torch
+    return [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            for _ in range(n)]
+
+
+def _rel_l2_dev(a, b):
+    return float((a - b).norm() / b.norm())
+
+
 # ---------------------------------------------------------------------------
-# workloads
+# the default workload: four1, nn = 2^28
+# ---------------------------------------------------------------------------
+def large_config(log2n, form):
+    nn = 1 << log2n
+    return {"workload": "four1 complex FFT, nn=2^%d (%d MiB of interleaved f64), i.i.d. N(0,1) "
+                        "from the seeded generator; one step = one in-place forward transform"
+                        % (log2n, (16 * nn) >> 20),
+            "form": form,
+            "l2": "input (%d MiB) larger than L2 (129 MB); no flush needed" % ((16 * nn) >> 20)}
+
+
+def large_input(log2n):
+    from numrs_gb300 import workloads as W
+    return W.normal(W.BASE_SEED + 5, 2 * (1 << log2n))
+
+
+def cpu_four1_sample(log2n, threads):
+    """One oracle four1 of 2^log2n points on `threads` threads; GFLOP/s."""
+    import oracle as O
+    from numrs_gb300 import workloads as W
+    nn = 1 << log2n
+    x = W.normal(W.BASE_SEED + 6, 2 * nn)
+    O.set_threads(threads)
+    w = W.normal(W.BASE_SEED + 7, 2 * 4096)
+    O.four1(w, 4096, 1)  # warm-up (pool threads, code)
+    t0 = time.perf_counter()
+    O.four1(x, nn, 1)
+    el = time.perf_counter() - t0
+    O.set_threads(1)
+    return 5.0 * nn * log2n / el / 1e9, el
+
+
+def run_large(args, world, rank, local):
+    import torch
+    import numrs_gb300 as nr
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    log2n = args.log2n or LARGE_LOG2N
+    nn = 1 << log2n
+    form = args.form
+    flops = 5.0 * nn * log2n
+    x = large_input(log2n)
+    x0 = torch.from_numpy(x).to(dev)  # the input, kept to restore between steps
+    d = torch.empty_like(x0)
+    stream = torch.cuda.current_stream()
+    nr.set_async(True)
+
+    def step(f):
+        nr.four1(d, nn, 1, form=f)
+
+    def timed(f, steps):
+        ev = _events(steps)
+        for i in range(steps):
+            d.copy_(x0)
+            ev[i][0].record(stream)
+            step(f)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev)
+
+    # the FP64 form's output: the yardstick of the other forms (the FP64 form
+    # itself is held to the CPU oracle at 1e-12 by the parity tests)
+    d.copy_(x0)
+    step("fp64")
+    torch.cuda.synchronize()
+    ref64 = d.clone()
+    for _ in range(max(args.warmup, 3)):
+        d.copy_(x0)
+        step(form)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----
+    clocks = Clocks(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    nr.launch_count(reset=True)
+    total_ms = timed(form, args.steps)
+    launches = nr.launch_count()
+    clk = clocks.stop()
+    barrier(world)
+    total_ms = max_over_ranks(total_ms, world)
+    value = flops * args.steps * world / (total_ms / 1e3) / 1e9
+    acc_main = None if form == "fp64" else _rel_l2_dev(d, ref64)
+
+    # ---- per-kernel event timing (a separate profiled repetition) ----
+    nr.profile(True)
+    for _ in range(min(args.steps, 10)):
+        d.copy_(x0)
+        step(form)
+    torch.cuda.synchronize()
+    pass_ms, pass_n, pass_bytes, pass_flops = nr.profile_read("pass")
+    nr.profile(False)
+
+    # ---- the other arithmetic forms on the same step ----
+    forms = {}
+    if not args.no_forms and rank == 0:
+        for f in ("fp64", "df64", "fp32", "tc32"):
+            if f == form:
+                continue
+            for _ in range(3):
+                d.copy_(x0)
+                step(f)
+            k = min(args.steps, 10)
+            ms = timed(f, k)
+            forms[f] = {"value": flops * k / (ms / 1e3) / 1e9, "unit": "GFLOP/s",
+                        "ms_per_step": ms / k,
+                        "rel_l2_vs_fp64_form": None if f == "fp64" else _rel_l2_dev(d, ref64)}
+    nr.set_async(False)
+    del d
+    torch.cuda.empty_cache()
+
+    # ---- end to end through the C ABI on a pinned host array ----
+    xh = torch.from_numpy(x).pin_memory()
+    xn = xh.numpy()
+    e2e_steps = max(3, min(args.steps, 5))
+    nr.four1(xn, nn, 1, form=form)  # warm-up (staging buffers)
+    e2e_s = 0.0
+    barrier(world)
+    for _ in range(e2e_steps):
+        xh.copy_(torch.from_numpy(x))
+        t0 = time.perf_counter()
+        nr.four1(xn, nn, 1, form=form)
+        e2e_s += time.perf_counter() - t0
+    e2e_s = max_over_ranks(e2e_s, world)
+    e2e_val = flops * e2e_steps * world / e2e_s / 1e9
+    e2e_acc = _rel_l2_dev(torch.from_numpy(xn).to(dev), ref64)
+    del xh, xn, x0
+    torch.cuda.empty_cache()
+
+    # ---- the batched target (20,000 uneven transforms) ----
+    batch = None
+    if not args.no_batch:
+        batch = batch_target(args, dev, rank, world)
+    if rank != 0:
+        return None
+
+    # ---- CPU baseline: the oracle on a bounded sample (2^26 points) ----
+    cores = host_cores()
+    cpu_all, el_all = cpu_four1_sample(26, cores)
+    cpu_one, el_one = cpu_four1_sample(26, 1)
+
+    hbm, hbm_kind = peaks()
+    pass_avg_ms = pass_ms / max(pass_n, 1)
+    per_launch = pass_bytes / max(pass_n, 1)
+    achieved = per_launch / (pass_avg_ms / 1e3) / 1e9 if pass_n else 0.0
+    traffic, traffic_note = traffic_of("large", form)
+    cfg = large_config(log2n, form)
+    line = {
+        "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == "fp64" else form,
+        "data": "synthetic (seeded N(0,1) complex)",
+        "config": cfg,
+        "e2e": {"value": e2e_val, "unit": "GFLOP/s", "steps": e2e_steps,
+                "h2d_bytes_per_step": 16 * nn, "d2h_bytes_per_step": 16 * nn,
+                "host_buffers": "pinned", "rel_l2_vs_device_fp64": e2e_acc},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "traffic_note": traffic_note,
+                     "kernel": "k_pass (Stockham pass)",
+                     "peak_source": ("of measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_kind == "measured"
+                                     else "of fallback 6.8 TB/s"),
+                     "launches": pass_n, "avg_launch_ms": pass_avg_ms,
+                     "bytes_per_launch": per_launch,
+                     "bytes_rule": "32 B per point per pass (16 B read + 16 B written, f64 I/O; "
+                                   "8 B per side for FP32 scratch)"},
+        "compute_roofline": {"bound": "fp64" if form in ("fp64",) else "fp32",
+                             "achieved_tflops": pass_flops / (pass_ms / 1e3) / 1e12 if pass_ms else 0.0,
+                             "peak_tflops": FP64_PEAK_TFLOPS if form == "fp64" else FP32_PEAK_TFLOPS,
+                             "frac": ((pass_flops / (pass_ms / 1e3) / 1e12) /
+                                      (FP64_PEAK_TFLOPS if form == "fp64" else FP32_PEAK_TFLOPS))
+                             if pass_ms else 0.0,
+                             "note": "nominal 5 N log2 R per radix-R pass over the pass kernel's "
+                                     "event time; peaks from the DFMA / FFMA loop probes"},
+        "kernels": {"pass": {"ms": pass_ms, "launches": pass_n}},
+        "accuracy": {"rel_l2_vs_fp64_form": acc_main},
+        "forms": forms,
+        "batch_target": batch,
+        "cpu_baseline": {"value": cpu_all, "unit": "GFLOP/s", "cores": cores, "kind": "port",
+                         "sample": "one oracle four1 of 2^26 points (a quarter of the 2^28 "
+                                   "workload) on all %d host threads: %.1f s; GFLOP/s by "
+                                   "5 N log2 N" % (cores, el_all),
+                         "one_core": {"value": cpu_one, "seconds": el_one},
+                         "host_cores": cores,
+                         "build": "g++ -O3 -ffp-contract=off (portable flags, no -march)"},
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    return line
+
+
+# ---------------------------------------------------------------------------
+# the batched configuration: 20,000 transforms, 2^6..2^14 points
+# ---------------------------------------------------------------------------
+def batch_inputs():
+    from numrs_gb300 import workloads as W
+    sizes, u = W.batch_c3()
+    return sizes, W.batch_c3_data(sizes, u)
+
+
+def batch_target(args, dev, rank, world):
+    """Every form on the 20,000-transform batch: one persistent launch (a
+    CUDA-graph replay) per step, inputs restored between steps outside the
+    timed events.  Per-transform rel-L2 of every form against the FP64 form,
+    whose own per-transform error against the CPU oracle is reported too."""
+    import torch
+    import numrs_gb300 as nr
+    import oracle as O
+    sizes, host = batch_inputs()
+    flat = np.concatenate(host)
+    buf = torch.from_numpy(flat).to(dev)
+    orig = buf.clone()
+    starts = np.concatenate([[0], np.cumsum(2 * sizes)[:-1]])
+    views = [buf[int(s):int(s) + 2 * int(n)] for s, n in zip(starts, sizes)]
+    seg = torch.repeat_interleave(torch.arange(len(sizes), device=dev),
+                                  torch.from_numpy(2 * sizes).to(dev))
+    flops = float(sum(5.0 * s * math.log2(s) for s in sizes))
+    stream = torch.cuda.current_stream()
+
+    def seg_norms(v):
+        return torch.zeros(len(sizes), dtype=torch.float64, device=dev).index_add_(0, seg, v * v).sqrt()
+
+    nr.set_async(True)
+    res, outs = {}, {}
+    for f in ("fp64", "tc32", "fp32", "df64"):
+        b = nr.FFTBatch(views, form=f)
+        buf.copy_(orig)
+        b.run(1)
+        torch.cuda.synchronize()
+        outs[f] = buf.clone()
+        for _ in range(max(args.warmup, 3)):
+            buf.copy_(orig)
+            b.run(1)
+        steps = min(args.steps, 30)
+        ev = _events(steps)
+        nr.launch_count(reset=True)
+        for i in range(steps):
+            buf.copy_(orig)
+            ev[i][0].record(stream)
+            b.run(1)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        launches = nr.launch_count()
+        ms = max_over_ranks(sum(a.elapsed_time(c) for a, c in ev), world)
+        res[f] = {"ms_per_step": ms / steps, "transforms_per_s": len(sizes) * steps * world / (ms / 1e3),
+                  "value": flops * steps * world / (ms / 1e3) / 1e9, "unit": "GFLOP/s",
+                  "launches_per_step": launches / steps}
+    nr.set_async(False)
+    ref_n = seg_norms(outs["fp64"])
+    for f in ("tc32", "fp32", "df64"):
+        rel = (seg_norms(outs[f] - outs["fp64"]) / ref_n).cpu().numpy()
+        res[f]["rel_l2_vs_fp64_max"] = float(rel.max())
+        res[f]["rel_l2_vs_fp64_median"] = float(np.median(rel))
+    got64 = outs["fp64"].cpu().numpy()
+    del outs, buf, orig, seg
+    torch.cuda.empty_cache()
+    if rank != 0:
+        return None
+    # CPU oracle over all 20,000 transforms on every host thread: the batch's
+    # CPU baseline and the FP64 form's per-transform error against the oracle
+    threads = host_cores()
+    O.set_threads(threads)
+    refs = [a.copy() for a in host]
+    t0 = time.perf_counter()
+    O.fft_batch(refs, 1)
+    el = time.perf_counter() - t0
+    O.set_threads(1)
+    ref = np.concatenate(refs)
+    rel64 = np.sqrt(np.add.reduceat((got64 - ref) ** 2, starts)) / np.sqrt(np.add.reduceat(ref ** 2, starts))
+    res["fp64"]["rel_l2_vs_oracle_max"] = float(rel64.max())
+    ratio = res["tc32"]["transforms_per_s"] / res["fp64"]["transforms_per_s"]
+    return {
+        "workload": "batched uneven four1: 20,000 transforms, sizes 2^k with k uniform in 6..14, "
+                    "complex N(0,1) x 10^u, u ~ U[-3,3]; one persistent launch (CUDA graph) per step",
+        "forms": res,
+        "tc32_over_fp64_transforms_per_s": ratio,
+        "fp32_over_fp64_transforms_per_s": res["fp32"]["transforms_per_s"] / res["fp64"]["transforms_per_s"],
+        "target": "tensor-core form >= 3x the FP64 form's transforms/s at rel-L2 <= 1e-6 per transform",
+        "target_met": bool(ratio >= 3.0 and res["tc32"]["rel_l2_vs_fp64_max"] <= 1e-6),
+        "cpu_baseline": {"transforms_per_s": len(sizes) / el, "value": flops / el / 1e9,
+                         "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                         "sample": "all 20,000 transforms, one fft_batch call of the CPU oracle, "
+                                   "%.2f s" % el},
+    }
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the CPU oracle on the same configuration
+# ---------------------------------------------------------------------------
+def run_reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    if args.workload == "convlv":
+        return run_reference_convlv(args)
+    if args.workload not in ("large",):
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "the reference arm is provided for the large and convlv workloads"}))
+        return
+    import oracle as O
+    log2n = args.log2n or LARGE_LOG2N
+    nn = 1 << log2n
+    flops = 5.0 * nn * log2n
+    x = large_input(log2n)
+    threads = host_cores()
+    O.set_threads(threads)
+    from numrs_gb300 import workloads as W
+    w = W.normal(W.BASE_SEED + 7, 2 * (1 << 20))
+    for _ in range(max(0, min(args.warmup, 2))):
+        O.four1(w, 1 << 20, 1)  # warm-up on a 2^20 sample (pool threads, code)
+    budget = 150.0
+    steps, el = 0, 0.0
+    d = np.empty_like(x)
+    while steps < args.steps:
+        d[:] = x
+        t0 = time.perf_counter()
+        O.four1(d, nn, 1)
+        el += time.perf_counter() - t0
+        steps += 1
+        if el + el / steps > budget:
+            break
+    O.set_threads(1)
+    val = flops * steps / el / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "GFLOP/s", "n_gpus": args.gpus,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded N(0,1) complex)",
+        "config": large_config(log2n, "fp64"),
+        "requested_steps": args.steps,
+        "cpu_baseline": {"value": val, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                         "sample": "%d of %d requested steps, each one whole 2^%d-point four1 of "
+                                   "the CPU oracle (C++ restatement of FFT_1.rs:5-107), all %d "
+                                   "host threads; steps bounded by a %.0f s budget; warm-up on "
+                                   "2^20-point transforms" % (steps, args.steps, log2n, threads,
+                                                              budget)},
+        "e2e": {"value": val, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# convolution / correlation, N = 2^20
 # ---------------------------------------------------------------------------
 def convlv_inputs():
     from numrs_gb300 import workloads as W
@@ -184,6 +550,12 @@ CONV_N = 1 << 20
 CONV_FLOPS = 2 * 3 * 2.5 * CONV_N * 20  # two calls, three real FFTs each
 
 
+def convlv_config(form):
+    return {"workload": "realft convlv + correl, N=2^20 real f64, m=257 taps in a length-N "
+                        "wrap-around buffer; one step = one convlv and one correl",
+            "form": form, "l2": "flushed between timed steps (256 MiB write)"}
+
+
 def cpu_convlv_step(x, r, y):
     import oracle as O
     st, a = O.convlv(x, r, 1)
@@ -192,12 +564,12 @@ def cpu_convlv_step(x, r, y):
     return a, b
 
 
-def cpu_baseline(seconds, x, r, y):
+def cpu_baseline_convlv(seconds, x, r, y):
     """Time the CPU oracle on whole steps for about `seconds` of work.  Returns
     the baseline record and the oracle's outputs of the step, which the GPU
     results are checked against."""
     import oracle as O
-    threads = os.cpu_count() or 1
+    threads = host_cores()
     O.set_threads(threads)
     outs = cpu_convlv_step(x, r, y)  # warm-up
     n, t0 = 0, time.perf_counter()
@@ -210,19 +582,17 @@ def cpu_baseline(seconds, x, r, y):
     O.set_threads(1)
     return outs, {
         "value": CONV_FLOPS * n / el / 1e9, "unit": "GFLOP/s", "cores": min(2, threads),
-        "kind": "port",
+        "kind": "port", "host_cores": threads,
         "sample": "%d whole steps (convlv + correl, N=2^20) in %.1f s; the two forward "
                   "transforms of each call run on 2 threads as the reference's rayon::join "
                   "does, the transforms themselves are serial as in the crate" % (n, el),
     }
 
 
-def run_reference_arm(args, world, rank):
-    if rank != 0:
-        return
+def run_reference_convlv(args):
     x, r, y = convlv_inputs()
     import oracle as O
-    threads = os.cpu_count() or 1
+    threads = host_cores()
     O.set_threads(threads)
     for _ in range(max(0, min(args.warmup, 2))):
         cpu_convlv_step(x, r, y)
@@ -241,9 +611,7 @@ def run_reference_arm(args, world, rank):
         "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded N(0,1) signal, Gaussian-window response)",
-        "config": {"workload": "realft convlv + correl, N=2^20 real f64, m=257 taps in a "
-                               "length-N wrap-around buffer", "form": "fp64 (CPU)",
-                   "sampled_steps": steps, "requested_steps": args.steps},
+        "config": convlv_config("fp64"), "requested_steps": args.steps,
         "cpu_baseline": {"value": val, "unit": "GFLOP/s", "cores": min(2, threads), "kind": "port",
                          "sample": "%d of %d requested steps, CPU oracle (C++ restatement of "
                                    "Convolve.rs/Correlation.rs/Real_FT.rs)" % (steps, args.steps)},
@@ -363,7 +731,7 @@ def run_convlv(args, world, rank, local):
         return
     # ---- CPU baseline (rank 0, after every GPU leg); its outputs check the
     # accuracy of each form's run ----
-    (ra, rb), cpu = cpu_baseline(args.cpu_seconds, x, r, y)
+    (ra, rb), cpu = cpu_baseline_convlv(args.cpu_seconds, x, r, y)
     acc = {}
     for f, (ga, gb) in outputs.items():
         e = max(np.linalg.norm(ga - ra) / np.linalg.norm(ra),
@@ -380,16 +748,13 @@ def run_convlv(args, world, rank, local):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == "fp64" else form,
         "data": "synthetic (seeded N(0,1) signal, Gaussian-window response)",
-        "config": {"workload": "realft convlv + correl, N=2^20 real f64, m=257 taps in a "
-                               "length-N wrap-around buffer; one step = one convlv and one correl",
-                   "form": form, "l2": "flushed between timed steps (256 MiB write)",
-                   "nominal_flops_per_step": CONV_FLOPS},
+        "config": convlv_config(form), "nominal_flops_per_step": CONV_FLOPS,
         "e2e": {"value": e2e_val, "unit": "GFLOP/s", "steps": e2e_steps,
                 "h2d_bytes_per_step": 4 * CONV_N * 8, "d2h_bytes_per_step": 2 * CONV_N * 8,
                 "host_buffers": "pinned"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic_of("convlv", form)[0],
-                     "traffic_source": traffic_of("convlv", form)[1],
+                     "traffic_note": traffic_of("convlv", form)[1],
                      "kernel": "k_pass (Stockham pass)",
                      "peak_source": "%s MEASURED_PEAKS.json hbm_gbs" % hbm_kind if hbm_kind == "measured"
                      else "fallback 6.8 TB/s",
@@ -397,7 +762,7 @@ def run_convlv(args, world, rank, local):
                      "bytes_per_launch": pass_bytes / max(pass_n, 1)},
         "compute_roofline": {"bound": "fp64" if form == "fp64" else "fp32",
                              "achieved_tflops": pass_flops / (pass_ms / 1e3) / 1e12 if pass_ms else 0.0,
-                             "peak_tflops": FP64_PEAK_TFLOPS if form == "fp64" else 73.3,
+                             "peak_tflops": FP64_PEAK_TFLOPS if form == "fp64" else FP32_PEAK_TFLOPS,
                              "note": "nominal 5 N log2 R per pass over the pass-kernel time; peaks "
                                      "from the DFMA / FFMA probes"},
         "kernels": {"pass": {"ms": pass_ms, "launches": pass_n},
@@ -415,76 +780,52 @@ def run_convlv(args, world, rank, local):
 
 
 def run_four1(args, world, rank, local):
-    """One in-place complex FFT of 2^log2n points per step (device resident)."""
+    """One in-place complex FFT of 2^log2n points per step (device resident,
+    input restored between steps outside the timed events)."""
     import torch
     import numrs_gb300 as nr
     from numrs_gb300 import workloads as W
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    log2n = args.log2n or (28 if args.workload == "large" else 24)
+    log2n = args.log2n or 24
     nn = 1 << log2n
-    x = W.normal(W.BASE_SEED + 5, 2 * nn) if log2n <= 24 else None
-    d = torch.from_numpy(x).to(dev) if x is not None else torch.randn(2 * nn, dtype=torch.float64, device=dev)
-    acc = _accuracy_vs_fp64(args.form, d, lambda t, form: nr.four1(t, nn, 1, form=form))
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    x0 = torch.from_numpy(W.normal(W.BASE_SEED + 5, 2 * nn)).to(dev)
+    d = x0.clone()
+    acc = _accuracy_vs_fp64(args.form, x0, lambda t, form: nr.four1(t, nn, 1, form=form))
+    big = nn * 16 >= (256 << 20)
+    flush = None if big else torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     nr.set_async(True)
-    sign = [1]
 
     def step():
-        nr.four1(d, nn, sign[0], form=args.form)
-        sign[0] = -sign[0]
+        d.copy_(x0)
+        if flush is not None:
+            flush.zero_()
 
     for _ in range(max(args.warmup, 3)):
         step()
+        nr.four1(d, nn, 1, form=args.form)
     torch.cuda.synchronize()
-    stream = torch.cuda.current_stream()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
-    clocks = Clocks(local)
-    clocks.start()
-    time.sleep(0.3)
-    nr.launch_count(reset=True)
-    for i in range(args.steps):
-        if nn * 16 < (256 << 20):
-            flush.zero_()
-        ev[i][0].record(stream)
-        step()
-        ev[i][1].record(stream)
-    torch.cuda.synchronize()
-    launches = nr.launch_count()
-    clk = clocks.stop()
-    total_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), world)
+    total_ms, launches, clk = _timed_pre(args, local, step,
+                                         lambda: nr.four1(d, nn, 1, form=args.form), args.steps)
+    total_ms = max_over_ranks(total_ms, world)
     flops = 5.0 * nn * log2n
     nr.profile(True)
-    for i in range(min(args.steps, 20)):
+    for _ in range(min(args.steps, 20)):
         step()
+        nr.four1(d, nn, 1, form=args.form)
     torch.cuda.synchronize()
-    pass_ms, pass_n, pass_bytes, pass_flops = nr.profile_read("pass")
+    roof = _pass_roofline()
     nr.profile(False)
     nr.set_async(False)
     if rank != 0:
         return None
-    hbm, hbm_kind = peaks()
-    achieved = pass_bytes / (pass_ms / 1e3) / 1e9 if pass_ms else 0.0
-    return {
-        "metric": METRIC, "value": flops * args.steps * world / (total_ms / 1e3) / 1e9,
-        "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if args.form == "fp64" else args.form,
-        "data": "synthetic N(0,1) complex",
-        "config": {"workload": "four1 complex in-place FFT, N=2^%d (%d MiB), alternating isign"
-                               % (log2n, (16 * nn) >> 20), "form": args.form,
-                   "l2": "input larger than L2" if nn * 16 >= (256 << 20) else "flushed between steps"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic_of("four1_%d" % log2n, args.form)[0],
-                     "traffic_source": traffic_of("four1_%d" % log2n, args.form)[1],
-                     "kernel": "k_pass (Stockham pass)", "launches": pass_n, "avg_launch_ms": pass_ms / max(pass_n, 1),
-                     "bytes_per_launch": pass_bytes / max(pass_n, 1)},
-        "compute_roofline": {"bound": "fp64" if args.form == "fp64" else "fp32",
-                             "achieved_tflops": pass_flops / (pass_ms / 1e3) / 1e12 if pass_ms else 0.0,
-                             "peak_tflops": FP64_PEAK_TFLOPS if args.form == "fp64" else 73.3},
-        "accuracy": acc, "clocks": clk, "gpu_launches": launches,
-    }
+    t, note = traffic_of("four1_%d" % log2n, args.form)
+    roof["traffic"], roof["traffic_note"] = t, note
+    return _simple_line(args, world,
+                        "four1 complex in-place FFT, nn=2^%d (%d MiB), i.i.d. N(0,1)" % (log2n, (16 * nn) >> 20),
+                        flops, total_ms, args.steps, launches, clk,
+                        {"roofline": roof, "accuracy": acc,
+                         "l2": "input larger than L2" if big else "flushed between steps (256 MiB write)"})
 
 
 def _accuracy_vs_fp64(form, data, forward):
@@ -505,133 +846,68 @@ def _accuracy_vs_fp64(form, data, forward):
 
 
 def run_batch(args, world, rank, local):
-    """20,000 complex transforms of sizes 2^k, k uniform in 6..14, amplitudes
-    10^u (u uniform in [-3, 3]); one step = one batched call over all of them."""
+    """The 20,000-transform batch (sizes 2^k, k uniform in 6..14, amplitudes
+    10^u); one step = one batched call.  With several ranks the transforms are
+    partitioned by work (numrs_gb300.shard) and every rank runs its share:
+    the total work is fixed, so the scaling is strong."""
     import torch
     import numrs_gb300 as nr
-    from numrs_gb300 import workloads as W
+    from numrs_gb300 import shard
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    sizes, u = W.batch_c3()
-    host = W.batch_c3_data(sizes, u)
-    total = int(sum(2 * s for s in sizes))
-    buf = torch.empty(total, dtype=torch.float64, device=dev)
-    views, off = [], 0
-    for a in host:
-        v = buf[off:off + a.size]
-        v.copy_(torch.from_numpy(a))
-        views.append(v)
-        off += a.size
+    sizes_all, host_all = batch_inputs()
+    mine = shard.partition_by_work(sizes_all, world)[rank]
+    sizes = sizes_all[mine]
+    host = [host_all[i] for i in mine]
+    buf = torch.from_numpy(np.concatenate(host)).to(dev)
     orig = buf.clone()
-    flops = float(sum(5.0 * s * math.log2(s) for s in sizes))
-    nbytes = 2.0 * 8 * total
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    starts = np.concatenate([[0], np.cumsum(2 * sizes)[:-1]])
+    views = [buf[int(s):int(s) + 2 * int(n)] for s, n in zip(starts, sizes)]
+    flops_all = float(sum(shard.transform_work(s) for s in sizes_all))
+    nbytes = 2.0 * 8 * float(sum(2 * s for s in sizes_all))
     stream = torch.cuda.current_stream()
     nr.set_async(True)
-    results = {}
-    sample = list(range(0, len(sizes), max(1, len(sizes) // 200)))
-    # CPU baseline (rank 0): the oracle's FFTProcessor::fft_batch (one task per
-    # transform on all host threads) over the sampled transforms; its outputs
-    # check every form's accuracy
-    cpu, refs = None, {}
-    if rank == 0:
-        import oracle as O
-        threads = os.cpu_count() or 1
-        O.set_threads(threads)
-        arrs = [host[t].copy() for t in sample]
-        O.fft_batch(arrs, 1)  # warm-up
-        arrs = [host[t].copy() for t in sample]
-        t0 = time.perf_counter()
-        O.fft_batch(arrs, 1)
-        el = time.perf_counter() - t0
-        O.set_threads(1)
-        refs = dict(zip(sample, arrs))
-        sflops = float(sum(5.0 * sizes[t] * math.log2(sizes[t]) for t in sample))
-        cpu = {"value": sflops / el / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": "port",
-               "sample": "%d of the 20,000 transforms (every %d-th), one fft_batch call of the "
-                         "CPU oracle, %.3f s" % (len(sample), max(1, len(sizes) // 200), el)}
-    for form in [args.form] + ([f for f in ("fp64", "df64", "fp32", "tc32") if f != args.form]
-                               if not args.no_forms else []):
-        b = nr.FFTBatch(views, form=form)
+    b = nr.FFTBatch(views, form=args.form)
+    for _ in range(max(args.warmup, 3)):
         buf.copy_(orig)
         b.run(1)
-        torch.cuda.synchronize()
-        # accuracy on the sampled transforms, against the CPU baseline's outputs
-        errs = []
-        got = buf.cpu().numpy()
-        offs = np.concatenate([[0], np.cumsum(2 * sizes)])
-        for t in (sample if rank == 0 else []):
-            ref = refs[t]
-            g = got[offs[t]:offs[t + 1]]
-            errs.append(np.linalg.norm(g - ref) / np.linalg.norm(ref))
-        for _ in range(max(args.warmup, 3)):
-            b.run(1)
-        torch.cuda.synchronize()
-        steps = args.steps if form == args.form else min(args.steps, 50)
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-              for _ in range(steps)]
-        clocks = Clocks(local)
-        if form == args.form:
-            clocks.start()
-            time.sleep(0.3)
-        nr.launch_count(reset=True)
-        for i in range(steps):
-            flush.zero_()
-            ev[i][0].record(stream)
-            b.run(1)
-            ev[i][1].record(stream)
-        torch.cuda.synchronize()
-        launches = nr.launch_count()
-        clk = clocks.stop() if form == args.form else None
-        ms = max_over_ranks(sum(a.elapsed_time(c) for a, c in ev), world)
-        results[form] = {"value": flops * steps * world / (ms / 1e3) / 1e9, "unit": "GFLOP/s",
-                         "transforms_per_s": len(sizes) * steps * world / (ms / 1e3),
-                         "ms_per_step": ms / steps, "hbm_gbs": nbytes * steps / (ms / 1e3) / 1e9,
-                         "rel_l2_max": float(max(errs)) if errs else None,
-                         "rel_l2_median": float(np.median(errs)) if errs else None,
-                         "launches": launches, "clocks": clk}
+    torch.cuda.synchronize()
+    steps = args.steps
+    ev = _events(steps)
+    clocks = Clocks(local)
+    barrier(world)
+    clocks.start()
+    time.sleep(0.3)
+    nr.launch_count(reset=True)
+    for i in range(steps):
+        buf.copy_(orig)
+        ev[i][0].record(stream)
+        b.run(1)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    launches = nr.launch_count()
+    clk = clocks.stop()
+    ms = max_over_ranks(sum(a.elapsed_time(c) for a, c in ev), world)
     nr.set_async(False)
-    # end to end with host arrays: FFTBatch marshals the 20,000 pointers once,
-    # and each run is one library call on the caller's numpy arrays
-    hb = [a.copy() for a in host]
-    hbatch = nr.FFTBatch(hb, form=args.form)
-    hbatch.run(1)
-    e2e_steps = max(3, min(args.steps, 10))
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        hbatch.run(1)
-    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     if rank != 0:
         return None
     hbm, hbm_kind = peaks()
-    main_r = results[args.form]
-    line = {
-        "metric": METRIC, "value": main_r["value"], "unit": "GFLOP/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": main_r["ms_per_step"],
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.form == "fp64" else args.form,
-        "data": "synthetic complex N(0,1) x 10^u",
-        "config": {"workload": "batched uneven four1: 20000 transforms, sizes 2^k, k uniform "
-                               "in 6..14, one persistent launch (CUDA graph)", "form": args.form,
-                   "l2": "inputs (%.2f GB) larger than L2; L2 also flushed" % (nbytes / 2e9)},
-        "e2e": {"value": flops * e2e_steps * world / e2e_s / 1e9, "unit": "GFLOP/s",
-                "h2d_bytes_per_step": total * 8, "d2h_bytes_per_step": total * 8,
-                "host_buffers": "pageable numpy arrays through FFTBatch.run; the persistent "
-                                "kernel reads and writes them in place over the host link when "
-                                "they are 16-byte aligned (otherwise one packed staging copy "
-                                "each way)"},
-        "roofline": {"bound": "hbm", "achieved": main_r["hbm_gbs"], "peak": hbm, "unit": "GB/s",
-                     "frac": main_r["hbm_gbs"] / hbm, "traffic": traffic_of("batch", args.form)[0],
-                     "traffic_source": traffic_of("batch", args.form)[1],
-                     "kernel": "k_batch (persistent)"},
-        "forms": results, "cpu_baseline": cpu, "clocks": main_r["clocks"],
-        "gpu_launches": main_r["launches"],
-    }
-    return line
+    gbs = nbytes * steps / (ms / 1e3) / 1e9
+    t, note = traffic_of("batch", args.form)
+    return _simple_line(
+        args, world, "batched uneven four1: 20000 transforms, sizes 2^k, k uniform in 6..14, "
+        "one persistent launch (CUDA graph) per rank", flops_all, ms, steps, launches, clk,
+        {"transforms_per_s": len(sizes_all) * steps / (ms / 1e3),
+         "scaling": "strong",
+         "partition": "longest-processing-time by 5 nn log2 nn over %d rank(s); rank 0 holds "
+                      "%d transforms" % (world, len(mine)),
+         "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                      "frac": gbs / hbm, "traffic": t, "traffic_note": note,
+                      "kernel": "k_batch (persistent)"},
+         "l2": "inputs (2.33 GB) larger than L2"})
 
 
 def _simple_line(args, world, workload, flops, total_ms, steps, launches, clk, extra=None):
-    hbm, hbm_kind = peaks()
     line = {
         "metric": METRIC, "value": flops * steps * world / (total_ms / 1e3) / 1e9,
         "unit": "GFLOP/s", "n_gpus": world, "steps": steps, "warmup": args.warmup,
@@ -667,6 +943,27 @@ def _timed(args, local, step, flush, steps):
     return sum(a.elapsed_time(b) for a, b in ev), launches, clk
 
 
+def _timed_pre(args, local, pre, step, steps):
+    """As _timed, with pre() run before each step outside the timed events."""
+    import torch
+    import numrs_gb300 as nr
+    stream = torch.cuda.current_stream()
+    ev = _events(steps)
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    nr.launch_count(reset=True)
+    for i in range(steps):
+        pre()
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    launches = nr.launch_count()
+    clk = clocks.stop()
+    return sum(a.elapsed_time(b) for a, b in ev), launches, clk
+
+
 def _pass_roofline():
     import numrs_gb300 as nr
     hbm, _ = peaks()
@@ -678,37 +975,19 @@ def _pass_roofline():
             "fp64_tflops_nominal": fl / (ms / 1e3) / 1e12 if ms else 0.0}
 
 
-def _plane_wave_field(shape, dev, seed=0x6B3A2026 + 4, count=32):
-    """uniform[-1,1) plus `count` unit plane waves with integer wave vectors and
-    random phases, generated on the device (same construction as
-    numrs_gb300.workloads.plane_waves)."""
-    import torch
-    g = torch.Generator(device=dev)
-    g.manual_seed(seed)
-    x = torch.rand(shape, generator=g, device=dev, dtype=torch.float64) * 2 - 1
-    kv = (torch.rand((count, len(shape)), generator=g, device=dev, dtype=torch.float64) *
-          torch.tensor(shape, device=dev, dtype=torch.float64)).floor()
-    ph = 2 * math.pi * torch.rand(count, generator=g, device=dev, dtype=torch.float64)
-    grids = torch.meshgrid(*[torch.arange(s, device=dev, dtype=torch.float64) / s for s in shape],
-                           indexing="ij")
-    for c in range(count):
-        arg = sum(kv[c, d] * grids[d] for d in range(len(shape)))
-        x += torch.cos(2 * math.pi * arg + ph[c])
-    return x.contiguous()
-
-
 def run_nd(args, world, rank, local):
     """fourn 256 x 256 x 512 complex, or rlft3 512^3 real; forward + inverse per step."""
     import torch
     import numrs_gb300 as nr
+    from numrs_gb300 import workloads as W
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     nr.set_async(True)
     if args.workload == "fourn":
         shape = (256, 256, 512)
         n = int(np.prod(shape))
-        re = _plane_wave_field(shape, dev).reshape(-1)
-        im = _plane_wave_field(shape, dev, seed=0x6B3A2026 + 40).reshape(-1)
+        re = W.plane_waves_torch(shape, dev).reshape(-1)
+        im = W.plane_waves_torch(shape, dev, seed=W.BASE_SEED + 40).reshape(-1)
         d = torch.stack([re, im], dim=1).reshape(-1).contiguous()
         del re, im
         orig = d.clone()
@@ -722,7 +1001,7 @@ def run_nd(args, world, rank, local):
     else:
         shape = (512, 512, 512)
         n = int(np.prod(shape))
-        d = _plane_wave_field(shape, dev).reshape(-1)
+        d = W.plane_waves_torch(shape, dev).reshape(-1)
         orig = d.clone()
         sp = torch.zeros(512 * 2 * 512, dtype=torch.float64, device=dev)
 
@@ -860,18 +1139,14 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    if args.workload in ("four1", "large", "batch"):
-        fn = run_batch if args.workload == "batch" else run_four1
-        line = fn(args, world, rank, local)
-        if line:
-            print(json.dumps(line), flush=True)
-    elif args.workload in ("fourn", "rlft3", "c1", "convbatch"):
-        fn = {"c1": run_c1, "convbatch": run_convbatch}.get(args.workload, run_nd)
-        line = fn(args, world, rank, local)
-        if line:
-            print(json.dumps(line), flush=True)
-    else:
+    fn = {"large": run_large, "four1": run_four1, "batch": run_batch, "fourn": run_nd,
+          "rlft3": run_nd, "c1": run_c1, "convbatch": run_convbatch}.get(args.workload)
+    if fn is None:
         run_convlv(args, world, rank, local)
+    else:
+        line = fn(args, world, rank, local)
+        if line:
+            print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

@@ -84,6 +84,24 @@ int gbfft_set_autotune(int enable);
  * 3 = other.  bytes = algorithmic bytes moved by those launches, flops =
  * nominal 5 N log2 R of each radix-R pass over N points. */
 long long gbfft_launch_count(int reset);
+/* Failure injection for tests (no counterpart in the crate).  Keys:
+ *   GBFFT_DEBUG_FAIL_ALLOC_AT     the value-th device allocation from now on
+ *                                 fails as if the device were out of memory
+ *                                 (the call returns GBFFT_OOM); 0 = never
+ *   GBFFT_DEBUG_BATCH_SPIN_LIMIT  polls before a wait of the persistent batch
+ *                                 kernel gives up (0 = the default, 2^24)
+ *   GBFFT_DEBUG_BATCH_NEED_EXTRA  added to the tile count a pass-2 tile waits
+ *                                 for, so that its wait cannot be met and
+ *                                 must run out (the call returns
+ *                                 GBFFT_TIMEOUT); 0 = off
+ * The batch settings drop the cached batch plan.  Nothing here hangs or
+ * faults a GPU: every device wait stays bounded. */
+enum {
+  GBFFT_DEBUG_FAIL_ALLOC_AT = 1,
+  GBFFT_DEBUG_BATCH_SPIN_LIMIT = 2,
+  GBFFT_DEBUG_BATCH_NEED_EXTRA = 3
+};
+int gbfft_debug_set(int key, long long value);
 int gbfft_profile(int enable);  /* also clears the records */
 int gbfft_profile_read(int kind, double* ms, long long* launches, double* bytes,
                        double* flops);
@@ -100,17 +118,19 @@ int gbfft_four1_batch(double* const* ptrs, const size_t* nn, size_t count, int i
                       const gbfft_opts* opts);
 
 /* four1 that allocates nothing.  No counterpart in the crate: it serves
- * callers that cannot call cudaMalloc when they need a transform (code running
- * under CUDA graph capture, hosts with a fixed memory budget, plugins inside
- * another framework's memory pool).  Same transform as gbfft_four1 in FP64,
- * in place on DEVICE memory `data` (16-byte aligned), ordered on `stream`
+ * callers that cannot call cudaMalloc when they need a transform (hosts that
+ * fix their GPU memory budget up front, such as real-time or embedded
+ * systems, and plugins inside another framework's memory pool that may not
+ * allocate behind its back).  Same transform as gbfft_four1 in FP64, in place
+ * on DEVICE memory `data` (16-byte aligned), ordered on `stream`
  * (NULL = default).
  * Its scratch and twiddle tables are fixed arrays in the library image (about
  * 19 MiB held by every GPU that loads the library, until exit), so nn is
  * limited to 2^20 (GBFFT_UNSUPPORTED_SIZE above).  The first call on a device
- * sets it up and waits for that; make it before any stream capture.  Calls
- * share the scratch array: calls that overlap on the GPU race and must be
- * ordered by the caller. */
+ * sets it up and waits for that; make it before any stream capture (a first
+ * call on a capturing stream is refused with GBFFT_CUDA_ERROR).  Calls share
+ * the scratch array, which keeps the last call's contents: calls that overlap
+ * on the GPU race and must be ordered by the caller. */
 int gbfft_four1_noalloc(double* data, size_t nn, int isign, void* stream);
 
 /* Uniform batch: `count` transforms of nn points, `dist` doubles apart

@@ -59,7 +59,13 @@ SIGNATURES = {
     "gbfft_profile": [ctypes.c_int],
     "gbfft_set_autotune": [ctypes.c_int],
     "gbfft_profile_read": [ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_longlong), _dp, _dp],
+    "gbfft_debug_set": [ctypes.c_int, ctypes.c_longlong],
 }
+
+# gbfft_debug_set keys (failure injection for tests)
+DEBUG_FAIL_ALLOC_AT = 1
+DEBUG_BATCH_SPIN_LIMIT = 2
+DEBUG_BATCH_NEED_EXTRA = 3
 
 _lib = None
 

@@ -251,13 +251,8 @@ inline size_t pf_smem_bytes() {
 
 template <class F, int SG, int SIO>
 static cudaError_t prepare_pf_t() {
-  static bool done = false;
-  if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(k_batch_pf<F, SG, SIO>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)pf_smem_bytes<F>());
-  if (e == cudaSuccess) done = true;
-  return e;
+  static DeviceOnce done;
+  return smem_opt_in(k_batch_pf<F, SG, SIO>, pf_smem_bytes<F>(), done);
 }
 
 template <class F, int SG, int SIO>
@@ -277,17 +272,12 @@ static int occupancy_pf_t() {
   return n;
 }
 
-// Raise the dynamic shared memory limit of one instantiation (idempotent;
-// called before any stream capture).
+// Raise the dynamic shared memory limit of one instantiation on the current
+// device (once per device; called before any stream capture).
 template <class F, int SG, int SIO>
 static cudaError_t prepare_t() {
-  static bool done = false;
-  if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(k_batch<F, SG, SIO>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)pass_smem_bytes<F>(256));
-  if (e == cudaSuccess) done = true;
-  return e;
+  static DeviceOnce done;
+  return smem_opt_in(k_batch<F, SG, SIO>, pass_smem_bytes<F>(256), done);
 }
 
 template <class F, int SG, int SIO>

@@ -14,12 +14,38 @@
 // at most 4096 points take one launch; longer axes take 2-3 launches that
 // ping-pong through scratch, the last one writing the caller's array.
 #pragma once
+#include <atomic>
+
 #include "arith.cuh"
 #include "gbfft_internal.h"
 
 namespace gbfft {
 
 constexpr int kEPT = kTileEPT;  // complex elements per thread per tile
+
+// Devices on which a one-time per-kernel setting has been made.  Function
+// attributes belong to a device's context, so a process that launches on
+// several GPUs sets them on each one.  The bits are atomic: two host threads
+// whose first launches race both set the same attribute value, which is
+// harmless.  Devices 64 and above are set up on every launch.
+struct DeviceOnce {
+  std::atomic<unsigned long long> bits{0};
+};
+
+// Raise a kernel's dynamic shared memory limit to `smem` bytes on the current
+// device, once per device.
+template <class K>
+inline cudaError_t smem_opt_in(K kernel, size_t smem, DeviceOnce& once) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (once.bits.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (bit) once.bits.fetch_or(bit, std::memory_order_acq_rel);
+  return cudaSuccess;
+}
 
 // Shared-memory tile layout: column c, row r at c*cs + pidx(r).  The row
 // padding (one element per 2^sh) spreads strided accesses within a column
@@ -925,17 +951,14 @@ inline size_t pass_smem_bytes(int T) {
 }
 
 // Launch one k_pass instantiation; its dynamic shared memory limit is raised
-// once per instantiation (the static lives in this function template).
+// once per instantiation and device (the record lives in this function
+// template).
 template <class F, int SG, int IN, int OUT, int T>
 inline cudaError_t launch_pass_one(const PassParams& p, cudaStream_t st) {
-  static size_t attr_done = 0;
+  static DeviceOnce attr_done;
   const size_t smem = pass_smem_bytes<F>(T);
-  if (attr_done < smem) {
-    cudaError_t e = cudaFuncSetAttribute(k_pass<F, SG, IN, OUT, T>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_done = smem;
-  }
+  cudaError_t e = smem_opt_in(k_pass<F, SG, IN, OUT, T>, smem, attr_done);
+  if (e != cudaSuccess) return e;
   if (p.tiles <= 0 || p.tiles > 0x7FFFFFFFll) return cudaErrorInvalidValue;  // grid.x limit
   PassParams q = p;
   set_slot_offsets(q, T);

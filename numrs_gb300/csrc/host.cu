@@ -65,6 +65,13 @@ struct Ctx {
   bool profiling = false;
   std::vector<ProfRec> prof;
   std::vector<cudaEvent_t> evpool;
+  // Failure injection (gbfft_debug_set): fail the k-th device allocation
+  // counted from the setting (0 = never); the persistent batch kernel's poll
+  // limit (0 = the default) and an addition to its pass-2 wait targets.
+  long long fail_alloc_at = 0;
+  long long alloc_calls = 0;
+  unsigned int dbg_spin_limit = 0;
+  unsigned int dbg_need_extra = 0;
 };
 
 Ctx g;
@@ -102,6 +109,22 @@ unsigned long long npow2(unsigned long long x) {
   return p;
 }
 
+// Every device allocation of the library goes through here, so that a test
+// can make the k-th one fail (gbfft_debug_set) and check that the call
+// reports GBFFT_OOM and that the library works afterwards.
+cudaError_t dev_alloc(void** p, size_t bytes) {
+  if (g.fail_alloc_at > 0 && ++g.alloc_calls == g.fail_alloc_at) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();  // clear the (non-sticky) allocation error
+  }
+  return e;
+}
+
 int ensure(DevBuf& b, size_t bytes) {
   if (b.bytes >= bytes) return GBFFT_OK;
   if (b.p) {
@@ -111,11 +134,9 @@ int ensure(DevBuf& b, size_t bytes) {
     b.bytes = 0;
   }
   size_t want = std::max(bytes, (size_t)1 << 20);
-  cudaError_t e = cudaMalloc(&b.p, want);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
+  cudaError_t e = dev_alloc(&b.p, want);
+  if (e != cudaSuccess)
     return fail(GBFFT_OOM, "cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
-  }
   b.bytes = want;
   return GBFFT_OK;
 }
@@ -151,12 +172,22 @@ int init_locked(int device) {
 
 int tables(Form f, Twiddles& tw) {
   if (f == FORM_TC32) f = FORM_F32;  // the tensor-core form uses the FP32 tables
-  if (!g.tw_dense[f]) {
+  if (!g.tw_dense[f] || !g.tw_part[f]) {
+    // both tables or neither: a failed allocation leaves none behind
     size_t esz = (f == FORM_F32) ? 8 : 16;
-    CK(cudaMalloc(&g.tw_dense[f], kDenseEntries * esz));
-    CK(cudaMalloc(&g.tw_part[f], kPartialEntries * esz));
-    CK(launch_twiddles(f, g.tw_dense[f], g.tw_part[f], g.cur));
+    void* dense = nullptr;
+    void* part = nullptr;
+    cudaError_t e = dev_alloc(&dense, kDenseEntries * esz);
+    if (e == cudaSuccess) e = dev_alloc(&part, kPartialEntries * esz);
+    if (e != cudaSuccess) {
+      if (dense) cudaFree(dense);
+      return fail(e == cudaErrorMemoryAllocation ? GBFFT_OOM : GBFFT_CUDA_ERROR,
+                  "twiddle tables: cudaMalloc failed: %s", cudaGetErrorString(e));
+    }
+    CK(launch_twiddles(f, dense, part, g.cur));
     g.launches++;
+    g.tw_dense[f] = dense;
+    g.tw_part[f] = part;
   }
   tw.dense = g.tw_dense[f];
   tw.partial = g.tw_part[f];
@@ -428,10 +459,7 @@ int tune_tile(Form f, long long L, long long s, long long nlines, int lq_log, lo
   const size_t span = (s == 1) ? (size_t)((nlines - 1) * lstride + L) : (size_t)(nlines * L);
   if (span * 16 > (size_t(512) << 20) || L <= 64) return 12;
   void* tmp = nullptr;
-  if (cudaMalloc(&tmp, span * 16) != cudaSuccess) {
-    cudaGetLastError();
-    return 12;
-  }
+  if (dev_alloc(&tmp, span * 16) != cudaSuccess) return 12;
   cudaMemsetAsync(tmp, 0, span * 16, g.cur);
   cudaEvent_t a, b;
   cudaEventCreate(&a);
@@ -763,7 +791,7 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
       r2.p.out_ptrs = (void* const*)(dtab + bn.first);
       r2.kind = 2;
       r2.first = bn.first;
-      r2.need = (unsigned int)(r1.p.tiles / bn.count);
+      r2.need = (unsigned int)(r1.p.tiles / bn.count) + g.dbg_need_extra;
       first_pass.push_back(r1);
       second_pass.push_back(r2);
     }
@@ -792,7 +820,7 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
   b.P.head = (unsigned long long*)b.flags.p;
   b.P.err = (int*)((char*)b.flags.p + 8);
   b.P.done = (unsigned int*)b.done.p;
-  b.P.spin_limit = 1u << 24;
+  b.P.spin_limit = g.dbg_spin_limit ? g.dbg_spin_limit : (1u << 24);
   int dev_sms = 0;
   CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, g.device));
   // The prefetching kernel (opt-in: GBFFT_BATCH_PREFETCH=1) needs 16-byte
@@ -999,6 +1027,27 @@ int gbfft_profile_read(int kind, double* ms, long long* launches, double* bytes,
   if (bytes) *bytes = by;
   if (flops) *flops = fl;
   return GBFFT_OK;
+}
+
+int gbfft_debug_set(int key, long long value) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  switch (key) {
+    case GBFFT_DEBUG_FAIL_ALLOC_AT:
+      if (value < 0) return fail(GBFFT_INVALID_ARG, "debug_set: negative allocation index");
+      g.fail_alloc_at = value;
+      g.alloc_calls = 0;
+      return GBFFT_OK;
+    case GBFFT_DEBUG_BATCH_SPIN_LIMIT:
+    case GBFFT_DEBUG_BATCH_NEED_EXTRA:
+      if (value < 0 || value > 0xFFFFFFFFll) return fail(GBFFT_INVALID_ARG, "debug_set: value out of range");
+      if (key == GBFFT_DEBUG_BATCH_SPIN_LIMIT) g.dbg_spin_limit = (unsigned int)value;
+      else g.dbg_need_extra = (unsigned int)value;
+      // the cached batch plan (and its graph) holds the old values
+      batch_plan_free(g_batch);
+      return GBFFT_OK;
+    default:
+      return fail(GBFFT_INVALID_ARG, "debug_set: unknown key %d", key);
+  }
 }
 
 long long gbfft_launch_count(int reset) {

@@ -1,14 +1,15 @@
 // noalloc.cu -- gbfft_four1_noalloc: the complex FFT of gbfft_four1 for
 // callers that must not allocate GPU memory.
 //
-// Some callers cannot call cudaMalloc at the moment they need an FFT: code
-// that runs while a CUDA graph is being captured, real-time or embedded hosts
-// that fix their memory budget before the first frame, and plugins that live
-// inside another framework's memory pool.  gbfft_four1 takes its ping-pong
-// scratch and its twiddle tables from the library's allocator; this entry
-// point takes them from arrays of fixed size that are part of the library
-// image (file-scope __device__ arrays below).  Every GPU that loads the
-// library holds them (about 19 MiB) until the process exits.
+// Some callers cannot call cudaMalloc at the moment they need an FFT: hosts
+// that fix their GPU memory budget before the first frame (real-time and
+// embedded systems, whose allocator may not be entered later), and plugins
+// that live inside another framework's memory pool and may not allocate
+// behind its back.  gbfft_four1 takes its ping-pong scratch and its twiddle
+// tables from the library's allocator; this entry point takes them from
+// arrays of fixed size that are part of the library image (file-scope
+// __device__ arrays below).  Every GPU that loads the library holds them
+// (about 19 MiB) until the process exits.
 //
 // Limits and rules:
 //   - nn is a power of two with nn <= 2^20; larger sizes are rejected with
@@ -17,11 +18,14 @@
 //     FP64, on `stream`
 //   - the first call on a device sets that device up (looks up the arrays'
 //     device addresses and fills the twiddle table, then waits for the fill);
-//     make that first call before any stream capture
-//   - all calls share the one scratch array: calls that overlap on the GPU
-//     (other streams, or a second host thread) race on it and must be ordered
-//     by the caller.  The scratch is fully written before it is read in every
-//     call, so nothing needs clearing between calls.
+//     make that first call before any stream capture.  A first call made on a
+//     capturing stream is refused with GBFFT_CUDA_ERROR before anything is
+//     launched.
+//   - all calls share the one scratch array, which keeps what the last call
+//     left in it: calls that overlap on the GPU (other streams, or a second
+//     host thread) race on it and must be ordered by the caller.  Every call
+//     writes the scratch fully before it reads it, so nothing needs clearing
+//     between calls.
 #include <mutex>
 
 #include "../../include/gbfft.h"
@@ -76,22 +80,35 @@ __global__ void k_noalloc_twiddles(d2* dense, d2* partial) {
   }
 }
 
-int setup_device(int dev, cudaStream_t st, NoAllocDevice** out) {
-  if (dev < 0 || dev >= kMaxDevices) return GBFFT_CUDA_ERROR;
+// Set up device `dev` (the current device) on its first call.  Returns a
+// message on failure, nullptr on success.
+const char* setup_device(int dev, cudaStream_t st, NoAllocDevice** out) {
+  if (dev < 0 || dev >= kMaxDevices) return "four1_noalloc: device index beyond 63";
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
   NoAllocDevice& d = g_noalloc_dev[dev];
   if (!d.ready) {
+    // The set-up launches a fill kernel and waits for it, which a stream
+    // under capture cannot do: refuse before launching anything.
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+      cudaGetLastError();
+      return "four1_noalloc: cannot query the stream's capture state";
+    }
+    if (cs != cudaStreamCaptureStatusNone)
+      return "four1_noalloc: the first call on a device must not be made under stream capture";
     if (cudaGetSymbolAddress((void**)&d.scratch, g_noalloc_scratch) != cudaSuccess ||
         cudaGetSymbolAddress((void**)&d.dense, g_noalloc_tw_dense) != cudaSuccess ||
-        cudaGetSymbolAddress((void**)&d.partial, g_noalloc_tw_partial) != cudaSuccess)
-      return GBFFT_CUDA_ERROR;
+        cudaGetSymbolAddress((void**)&d.partial, g_noalloc_tw_partial) != cudaSuccess) {
+      cudaGetLastError();
+      return "four1_noalloc: cudaGetSymbolAddress failed";
+    }
     k_noalloc_twiddles<<<256, 256, 0, st>>>(d.dense, d.partial);
-    if (cudaGetLastError() != cudaSuccess) return GBFFT_CUDA_ERROR;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return GBFFT_CUDA_ERROR;
+    if (cudaGetLastError() != cudaSuccess) return "four1_noalloc: twiddle fill launch failed";
+    if (cudaStreamSynchronize(st) != cudaSuccess) return "four1_noalloc: twiddle fill failed";
     d.ready = true;
   }
   *out = &d;
-  return GBFFT_OK;
+  return nullptr;
 }
 
 // One pass of the Stockham schedule of a single line of L points (the same
@@ -168,8 +185,8 @@ extern "C" int gbfft_four1_noalloc(double* data, size_t nn, int isign, void* str
     return GBFFT_CUDA_ERROR;
   }
   NoAllocDevice* d = nullptr;
-  if (setup_device(dev, st, &d) != GBFFT_OK) {
-    record_error(GBFFT_CUDA_ERROR, "four1_noalloc: device set-up failed");
+  if (const char* msg = setup_device(dev, st, &d)) {
+    record_error(GBFFT_CUDA_ERROR, msg);
     return GBFFT_CUDA_ERROR;
   }
   if (nn == 1) return GBFFT_OK;

@@ -32,15 +32,28 @@ def uniform_pm1(seed, n):
 
 
 def normal(seed, n):
-    """i.i.d. N(0, 1) by Box-Muller on pairs of uniforms."""
+    """i.i.d. N(0, 1) by Box-Muller on pairs of uniforms.  Large arrays are
+    generated in chunks of pairs on several threads (numpy releases the GIL in
+    its element-wise kernels); every pair depends on its counter alone."""
     m = (n + 1) // 2
-    u1 = uniform(seed, m, 0)
-    u2 = uniform(seed, m, m)
-    r = np.sqrt(-2.0 * np.log1p(-u1))  # 1-u1 in (0, 1]
-    t = 2.0 * np.pi * u2
     out = np.empty(2 * m)
-    out[0::2] = r * np.cos(t)
-    out[1::2] = r * np.sin(t)
+
+    def pairs(a, b):
+        u1 = uniform(seed, b - a, a)
+        u2 = uniform(seed, b - a, m + a)
+        r = np.sqrt(-2.0 * np.log1p(-u1))  # 1-u1 in (0, 1]
+        t = 2.0 * np.pi * u2
+        out[2 * a:2 * b:2] = r * np.cos(t)
+        out[2 * a + 1:2 * b:2] = r * np.sin(t)
+
+    chunk = 1 << 21
+    if m <= chunk:
+        pairs(0, m)
+    else:
+        import concurrent.futures as cf
+        import os
+        with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+            list(ex.map(lambda a: pairs(a, min(m, a + chunk)), range(0, m, chunk)))
     return out[:n]
 
 
@@ -90,3 +103,28 @@ def plane_waves(shape, count=32, seed=BASE_SEED + 4):
         arg = sum(kv[c, d] * grids[d] for d in range(len(shape)))
         x = x + np.cos(2 * np.pi * arg + ph[c])
     return x
+
+
+def plane_waves_torch(shape, device, seed=BASE_SEED + 4, count=32):
+    """The same construction as plane_waves (uniform[-1,1) plus `count` unit
+    plane waves with integer wave vectors and random phases), generated on a
+    torch device with torch's seeded generator: fast enough for the 512^3
+    fields of the 3-D configurations."""
+    import math
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    x = torch.rand(shape, generator=g, device=device, dtype=torch.float64) * 2 - 1
+    kv = (torch.rand((count, len(shape)), generator=g, device=device, dtype=torch.float64) *
+          torch.tensor(shape, device=device, dtype=torch.float64)).floor()
+    ph = 2 * math.pi * torch.rand(count, generator=g, device=device, dtype=torch.float64)
+    grids = [torch.arange(s, device=device, dtype=torch.float64) / s for s in shape]
+    for c in range(count):
+        arg = None
+        for d in range(len(shape)):
+            view = [1] * len(shape)
+            view[d] = shape[d]
+            term = (kv[c, d] * grids[d]).reshape(view)
+            arg = term if arg is None else arg + term
+        x += torch.cos(2 * math.pi * arg + ph[c])
+    return x.contiguous()

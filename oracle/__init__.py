@@ -50,6 +50,7 @@ def lib():
         L.orc_magnitude_spectrum.argtypes = [_dp, _sz, _dp]
         L.orc_power_spectrum.argtypes = [_dp, _sz, _dp]
         L.orc_dft_ld.argtypes = [_dp, _sz, ctypes.c_int, _dp]
+        L.orc_dft_bins.argtypes = [_dp, _sz, ctypes.c_int, ctypes.POINTER(_sz), _sz, _dp]
         _lib = L
     return _lib
 
@@ -178,3 +179,14 @@ def dft_ld(data, nn, isign):
     out = np.zeros(2 * nn)
     lib().orc_dft_ld(_ptr(data), nn, isign, _ptr(out))
     return out
+
+
+def dft_bins(data, nn, isign, bins):
+    """Bins X_k (k in ``bins``) of the direct DFT of ``data`` (nn interleaved
+    complex values), each a compensated sum accurate to about one rounding.
+    Returns a complex128 array.  Uses the oracle's thread pool."""
+    bins = [int(b) for b in bins]
+    arr = (_sz * len(bins))(*bins)
+    out = np.zeros(2 * len(bins))
+    lib().orc_dft_bins(_ptr(data), nn, isign, arr, len(bins), _ptr(out))
+    return out[0::2] + 1j * out[1::2]

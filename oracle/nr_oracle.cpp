@@ -68,8 +68,9 @@ class Pool {
   }
   int size() const { return nthreads_; }
   // Run fn(i) for i in [0, count), spread over the pool; returns when all done.
+  // A call made from inside a pool task runs serially in that task.
   void parallel_for(size_t count, const std::function<void(size_t)>& fn) {
-    if (nthreads_ == 1 || count < 2) {
+    if (nthreads_ == 1 || count < 2 || t_in_task) {
       for (size_t i = 0; i < count; ++i) fn(i);
       return;
     }
@@ -89,12 +90,15 @@ class Pool {
 
  private:
   void work() {
+    t_in_task = true;
     for (;;) {
       size_t i = next_.fetch_add(1);
       if (i >= count_) break;
       (*job_)(i);
     }
+    t_in_task = false;
   }
+  static thread_local bool t_in_task;
   void loop(int) {
     uint64_t seen = 0;
     for (;;) {
@@ -119,6 +123,8 @@ class Pool {
   uint64_t gen_ = 0;
   bool stop_ = false;
 };
+
+thread_local bool Pool::t_in_task = false;
 
 Pool* g_pool = nullptr;
 Pool& pool() {
@@ -407,10 +413,16 @@ static void fourn_impl(double* data, const size_t* nn, size_t ndim, int isign) {
   for (size_t dd = ndim; dd-- > 0;) {
     size_t len = nn[dd];
     if (len == 1) continue;
-    size_t outer = total / (len * stride);
-    std::vector<double> line(2 * len);
-    for (size_t o = 0; o < outer; ++o) {
-      for (size_t s = 0; s < stride; ++s) {
+    const size_t outer = total / (len * stride);
+    // Lines are independent, so they are spread over the pool (in groups of
+    // consecutive lines); each line's arithmetic is the same whatever the
+    // thread count.
+    const size_t lines = outer * stride;
+    const size_t group = std::max<size_t>(1, std::min<size_t>(64, lines / 256));
+    pool().parallel_for((lines + group - 1) / group, [&](size_t gi) {
+      std::vector<double> line(2 * len);
+      for (size_t li = gi * group; li < std::min(lines, (gi + 1) * group); ++li) {
+        const size_t o = li / stride, s = li % stride;
         double* base = data + 2 * (o * len * stride + s);
         for (size_t l = 0; l < len; ++l) {
           line[2 * l] = base[2 * l * stride];
@@ -422,7 +434,7 @@ static void fourn_impl(double* data, const size_t* nn, size_t ndim, int isign) {
           base[2 * l * stride + 1] = line[2 * l + 1];
         }
       }
-    }
+    });
     stride *= len;
   }
 }
@@ -784,6 +796,84 @@ void orc_magnitude_spectrum(const double* c, size_t nn, double* out) {
 }
 void orc_power_spectrum(const double* c, size_t nn, double* out) {
   for (size_t k = 0; k < nn; ++k) out[k] = c[2 * k] * c[2 * k] + c[2 * k + 1] * c[2 * k + 1];
+}
+
+// ---------------------------------------------------------------------------
+// Exact-arithmetic spot checks at full size: selected bins X_k of a direct
+// DFT, X_k = sum_j x_j exp(+2 pi i isign jk/nn), evaluated with compensated
+// (twice-working-precision) dot products, so that each bin is accurate to
+// about one rounding of its magnitude whatever nn is.  Independent of every
+// FFT in this file and in the library.
+// ---------------------------------------------------------------------------
+// exp(2 pi i m / nn), 0 <= m < nn, nn a power of two, with the angle reduced
+// to [0, pi/4] before cos/sin so that each value is within about one ulp.
+static void unit_root(size_t m, size_t nn, double& c, double& s) {
+  bool neg_s = false, neg_c = false, swap = false;
+  if (m > nn / 2) { m = nn - m; neg_s = true; }   // exp(i(2 pi - a)) = conj exp(ia)
+  if (m > nn / 4) { m = nn / 2 - m; neg_c = true; }  // exp(i(pi - a)) = -cos a + i sin a
+  if (m > nn / 8) { m = nn / 4 - m; swap = true; }   // cos(pi/2 - a) = sin a
+  const double a = 2.0 * PI * (double)m / (double)nn;
+  double cc = std::cos(a), ss = std::sin(a);
+  if (swap) std::swap(cc, ss);
+  c = neg_c ? -cc : cc;
+  s = neg_s ? -ss : ss;
+}
+
+// Error-free transformations: a + b = s + e exactly (Knuth's TwoSum) and
+// a * b = p + e exactly (through a fused multiply-add).
+static inline void two_sum(double a, double b, double& s, double& e) {
+  s = a + b;
+  const double bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+static inline void two_prod(double a, double b, double& p, double& e) {
+  p = a * b;
+  e = std::fma(a, b, -p);
+}
+
+// Compensated complex accumulator: (sr + cr) + i (si + ci).
+struct CAcc {
+  double sr = 0, cr = 0, si = 0, ci = 0;
+  inline void add_prod(double ar, double ai, double br, double bi) {
+    double p, e, t, f;
+    two_prod(ar, br, p, e); two_sum(sr, p, t, f); sr = t; cr += e + f;
+    two_prod(-ai, bi, p, e); two_sum(sr, p, t, f); sr = t; cr += e + f;
+    two_prod(ar, bi, p, e); two_sum(si, p, t, f); si = t; ci += e + f;
+    two_prod(ai, br, p, e); two_sum(si, p, t, f); si = t; ci += e + f;
+  }
+};
+
+void orc_dft_bins(const double* in, size_t nn, int isign, const size_t* bins, size_t nb,
+                  double* out) {
+  // j = j1 + N1 j2: exp(2 pi i jk/nn) = A[j1] B[j2] with A[j1] = w^(j1 k),
+  // B[j2] = w^(N1 j2 k).  Inner sums over j1 and the outer sum over j2 are
+  // both compensated.
+  int lg = 0;
+  while ((size_t(1) << lg) < nn) ++lg;
+  const size_t N1 = size_t(1) << ((lg + 1) / 2), N2 = nn / N1;
+  const double sg = isign > 0 ? 1.0 : -1.0;
+  pool().parallel_for(nb, [&](size_t b) {
+    const size_t k = bins[b] % nn;
+    std::vector<double> ar(N1), ai(N1);
+    for (size_t j1 = 0; j1 < N1; ++j1) {
+      unit_root((j1 * k) % nn, nn, ar[j1], ai[j1]);
+      ai[j1] *= sg;
+    }
+    CAcc outer;
+    for (size_t j2 = 0; j2 < N2; ++j2) {
+      CAcc inner;
+      const double* x = in + 2 * j2 * N1;
+      for (size_t j1 = 0; j1 < N1; ++j1) inner.add_prod(x[2 * j1], x[2 * j1 + 1], ar[j1], ai[j1]);
+      double br, bi;
+      unit_root((N1 * ((j2 * k) % nn)) % nn, nn, br, bi);
+      bi *= sg;
+      // (s + c) * B: the rounded inner sum and its correction, each times B
+      outer.add_prod(inner.sr, inner.si, br, bi);
+      outer.add_prod(inner.cr, inner.ci, br, bi);
+    }
+    out[2 * b] = outer.sr + outer.cr;
+    out[2 * b + 1] = outer.si + outer.ci;
+  });
 }
 
 // Long-double direct DFT for small spot checks: X_k = sum_j x_j exp(+2 pi i isign jk/n).

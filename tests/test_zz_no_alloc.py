@@ -1,10 +1,13 @@
-"""gbfft_four1_noalloc against gbfft_four1.
+"""gbfft_four1_noalloc against gbfft_four1 and the oracle.
 
 The no-allocation entry point exists for callers that cannot call cudaMalloc
-when they need a transform (for example while a CUDA graph is being captured,
-or under a fixed memory budget).  It must give the same transform as the
-ordinary entry point.  This file is collected last so that a failure here
-leaves every other GPU test already run.
+when they need a transform: hosts that fix their GPU memory budget up front
+and plugins living inside another framework's memory pool.  It must give the
+same transform as the ordinary entry point, call after call (its scratch is
+one shared array that keeps the previous call's contents).  Every size it
+accepts is run, which covers its one-pass tiles and every two-pass radix
+split.  This file is collected last so that a failure here leaves every
+other GPU test already run.
 """
 import ctypes
 
@@ -25,12 +28,15 @@ def env():
     return torch, _lib, _lib.load()
 
 
-@pytest.mark.parametrize("log2n", [12, 16, 20])
+@pytest.mark.parametrize("log2n", list(range(0, 21)))
 @pytest.mark.parametrize("isign", [1, -1])
 def test_noalloc_matches_four1_twice(env, log2n, isign):
     torch, L, lib = env
+    import oracle as O
     nn = 1 << log2n
     x = W.normal(9000 + log2n, 2 * nn)
+    oracle_out = x.copy()
+    O.four1(oracle_out, nn, isign)
     # the ordinary entry point, on device memory
     ref = torch.from_numpy(x.copy()).cuda()
     o = L.Opts()
@@ -38,6 +44,7 @@ def test_noalloc_matches_four1_twice(env, log2n, isign):
     assert lib.gbfft_four1(ref.data_ptr(), nn, isign, ctypes.byref(o)) == L.OK, L.last_error()
     torch.cuda.synchronize()
     want = ref.cpu().numpy()
+    assert_fp64_close(want, oracle_out, log2n, "four1 vs oracle")
     # two calls in a row through the no-allocation entry point
     for call in range(2):
         t = torch.from_numpy(x.copy()).cuda()
@@ -45,7 +52,9 @@ def test_noalloc_matches_four1_twice(env, log2n, isign):
         st = lib.gbfft_four1_noalloc(t.data_ptr(), nn, isign, None)
         assert st == L.OK, L.last_error()
         torch.cuda.synchronize()
-        assert_fp64_close(t.cpu().numpy(), want, log2n, "four1_noalloc call %d" % call)
+        got = t.cpu().numpy()
+        assert_fp64_close(got, want, log2n, "four1_noalloc call %d vs four1" % call)
+        assert_fp64_close(got, oracle_out, log2n, "four1_noalloc call %d vs oracle" % call)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(env):
