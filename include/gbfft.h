@@ -78,6 +78,17 @@ int gbfft_release(void);
  * keeps the fastest (also GBFFT_AUTOTUNE=1; GBFFT_TUNE_CACHE=<file> keeps the
  * choices across processes).  Tuning synchronises the device once per shape. */
 int gbfft_set_autotune(int enable);
+/* Forward transforms of gbfft_convlv / gbfft_correl (no counterpart switch in
+ * the crate; the batched forms always use path 0, which transforms a shared
+ * response once):
+ *   0  the two real inputs as two n/2-point realft lines in one batched
+ *      launch sequence (the default)
+ *   1  the two real inputs packed as the real and imaginary parts of one
+ *      n-point complex FFT, as twofft does (src/FFT_2.rs:3-17), then one
+ *      kernel splits the two spectra, multiplies them and applies the
+ *      inverse realft twist
+ * Both give the same results within the parity bars. */
+int gbfft_set_spectral_path(int path);
 /* Instrumentation (no counterpart in the crate).  Kernel launches issued
  * since the last reset; optional event timing of every launch on its stream,
  * summed per kind: 0 = FFT passes, 1 = realft twists, 2 = spectral products,
@@ -132,6 +143,14 @@ int gbfft_four1_batch(double* const* ptrs, const size_t* nn, size_t count, int i
  * the scratch array, which keeps the last call's contents: calls that overlap
  * on the GPU race and must be ordered by the caller. */
 int gbfft_four1_noalloc(double* data, size_t nn, int isign, void* stream);
+
+/* FFTProcessor::fft followed by magnitude_spectrum (kind 0) or power_spectrum
+ * (kind 1): src/FFT_1.rs:166,206,218.  data (2*nn doubles) is transformed in
+ * place as gbfft_four1 does, and the transform's last pass also writes
+ * spec[k] = |X_k| or |X_k|^2 (k < nn) from the values it stores, so the
+ * spectrum costs no pass of its own over the data. */
+int gbfft_four1_spectrum(double* data, size_t nn, int isign, int kind, double* spec,
+                         const gbfft_opts* opts);
 
 /* Uniform batch: `count` transforms of nn points, `dist` doubles apart
  * (dist >= 2*nn). */

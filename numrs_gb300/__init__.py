@@ -35,6 +35,7 @@ __all__ = [
     "autocorrel", "magnitude_spectrum", "power_spectrum", "real_to_complex",
     "complex_to_real", "ConvlvError", "CorrelError", "GbfftError", "launch_count",
     "FFTBatch", "four1_many", "set_async", "profile", "profile_read", "four1_noalloc",
+    "four1_spectrum", "set_spectral_path",
     "correl_normalized", "correl_normalized_fast", "autocorrel_fast", "ConvlvProcessor",
     "RealFTProcessor", "TwoFFTProcessor",
 ]
@@ -171,10 +172,11 @@ def four1(data, nn, isign, form="fp64"):
 def four1_noalloc(data, nn, isign, stream=None):
     """four1 on a CUDA float64 tensor without any GPU memory allocation.
 
-    For callers that cannot allocate when they transform (graph capture,
-    fixed memory budgets): scratch and tables are fixed arrays inside the
-    library, so nn <= 2^20.  Calls that overlap on the GPU share that scratch;
-    order them.
+    For callers that cannot allocate when they transform (fixed GPU memory
+    budgets, plugins inside another framework's memory pool): scratch and
+    tables are fixed arrays inside the library, so nn <= 2^20.  The first call
+    on a device sets it up and must not be made under stream capture.  Calls
+    that overlap on the GPU share that scratch; order them.
     """
     a = _Arg(data, True)
     if not a.dev:
@@ -183,6 +185,23 @@ def four1_noalloc(data, nn, isign, stream=None):
         import torch
         stream = torch.cuda.current_stream().cuda_stream
     _check(_lib.load().gbfft_four1_noalloc(a.ptr, nn, isign, stream))
+
+
+def four1_spectrum(data, nn, isign, kind="magnitude", form="fp64", out=None):
+    """four1 in place, plus its magnitude (or power) spectrum written by the
+    transform's last pass: ``FFTProcessor::fft`` then ``magnitude_spectrum`` /
+    ``power_spectrum`` (src/FFT_1.rs:166,206,218) without a second pass over
+    the data.  Returns the spectrum (nn doubles)."""
+    a = _Arg(data, True)
+    if a.size < 2 * nn:
+        raise ValueError("data holds %d doubles, need 2*nn=%d" % (a.size, 2 * nn))
+    k = {"magnitude": 0, "power": 1}[kind]
+    if out is None:
+        out = _new_like(a, nn)
+    o = _opts([a, _Arg(out, True)], form)
+    _check(_lib.load().gbfft_four1_spectrum(a.ptr, nn, isign, k, _Arg(out, True).ptr,
+                                            ctypes.byref(o)))
+    return out
 
 
 def four1_optimized(data, nn, isign, form="fp64"):
@@ -579,6 +598,13 @@ def complex_to_real(c):
 def launch_count(reset=False):
     """Kernel launches issued by the library since the last reset."""
     return _lib.load().gbfft_launch_count(1 if reset else 0)
+
+
+def set_spectral_path(path):
+    """How convlv / correl transform their two real inputs: "realft" (two
+    n/2-point realft lines, the default) or "twofft" (packed as one n-point
+    complex FFT, src/FFT_2.rs:3-17, with a fused split-product-twist step)."""
+    _check(_lib.load().gbfft_set_spectral_path({"realft": 0, "twofft": 1}[path]))
 
 
 def set_autotune(enable=True):

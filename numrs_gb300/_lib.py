@@ -40,6 +40,7 @@ SIGNATURES = {
     "gbfft_four1": [_vp, _sz, ctypes.c_int, _op],
     "gbfft_four1_batch": [ctypes.POINTER(_vp), ctypes.POINTER(_sz), _sz, ctypes.c_int, _op],
     "gbfft_four1_many": [_vp, _sz, _sz, _sz, ctypes.c_int, _op],
+    "gbfft_four1_spectrum": [_vp, _sz, ctypes.c_int, ctypes.c_int, _vp, _op],
     "gbfft_twofft": [_vp, _vp, _vp, _vp, _sz, _op],
     "gbfft_realft": [_vp, _sz, ctypes.c_int, _op],
     "gbfft_fourn": [_vp, ctypes.POINTER(_sz), _sz, _sz, ctypes.c_int, _op],
@@ -60,6 +61,7 @@ SIGNATURES = {
     "gbfft_set_autotune": [ctypes.c_int],
     "gbfft_profile_read": [ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_longlong), _dp, _dp],
     "gbfft_debug_set": [ctypes.c_int, ctypes.c_longlong],
+    "gbfft_set_spectral_path": [ctypes.c_int],
 }
 
 # gbfft_debug_set keys (failure injection for tests)

@@ -208,6 +208,18 @@ __device__ __forceinline__ typename F::C apply_scale(typename F::C w, const Pass
   else return F::scale(w, p.scale);
 }
 
+// Spectrum epilogue of a transform's last pass (magnitude_spectrum and
+// power_spectrum, src/FFT_1.rs:206-228, fused into the store): spec[i] =
+// |X|^2 or its square root, in double, for the output element of index i.
+template <class F>
+__device__ __forceinline__ void spec_store(const PassParams& p, long long i,
+                                           const typename F::C& v) {
+  double x, y;
+  F::to_d(v, x, y);
+  const double pw = x * x + y * y;
+  p.spec[i] = p.spec_kind == 1 ? sqrt(pw) : pw;
+}
+
 // ---------------------------------------------------------------------------
 // Global element access with format conversion.
 // ---------------------------------------------------------------------------
@@ -337,16 +349,13 @@ __device__ __forceinline__ long long thread_base_out(const PassParams& p, long l
   return line_base(p, line0) + jd0 * p.s + col_off_out(p, c) + r * (p.Ns * p.s);
 }
 
-// The R-point DFTs of the tile's columns, then the store at the autosorted
-// positions.  Starts after a barrier that made the staged tile visible.
-template <class F, int SG, int OUT, int T>
-__device__ __forceinline__ void tile_compute_store(const PassParams& p, long long line0,
-                                                   long long j0, typename F::S* sm, int tid) {
-  using C = typename F::C;
-  using OE = typename IOElem<OUT>::T;
-  constexpr int sh = F::kPadShift;
-  const int logR = p.logR, logC = p.logC;
-  const int cs = col_stride(logR, sh);
+// The R-point DFTs of the tile's columns in shared memory: the pass's
+// sub-passes in order.  Starts after a barrier that made the tile visible and
+// ends with one.
+template <class F, int SG, int T>
+__device__ __forceinline__ void run_subpasses(const PassParams& p, typename F::S* sm, int cs,
+                                              int tid) {
+  const int logR = p.logR;
   int logNsub = 0;
   for (int k = 0; k < p.nq; ++k) {
     const int lq = p.q[k];
@@ -366,10 +375,24 @@ __device__ __forceinline__ void tile_compute_store(const PassParams& p, long lon
     }
     logNsub += lq;
   }
+}
+
+// The R-point DFTs of the tile's columns, then the store at the autosorted
+// positions.  Starts after a barrier that made the staged tile visible.
+template <class F, int SG, int OUT, int T>
+__device__ __forceinline__ void tile_compute_store(const PassParams& p, long long line0,
+                                                   long long j0, typename F::S* sm, int tid) {
+  using C = typename F::C;
+  using OE = typename IOElem<OUT>::T;
+  constexpr int sh = F::kPadShift;
+  const int logR = p.logR, logC = p.logC;
+  const int cs = col_stride(logR, sh);
+  run_subpasses<F, SG, T>(p, sm, cs, tid);
   if (p.out_ptrs == nullptr) {
     // linear layout: per-thread base plus the slot offsets out_off[k]
     long long ct;
-    OE* dst = reinterpret_cast<OE*>(p.out) + thread_base_out(p, line0, j0, tid, ct);
+    const long long tb = thread_base_out(p, line0, j0, tid, ct);
+    OE* dst = reinterpret_cast<OE*>(p.out) + tb;
     const long long rem = (p.mode == 0) ? (1ll << 62) : p.nlines - line0;
 #pragma unroll 4
     for (int k = 0; k < kEPT; ++k) {
@@ -382,6 +405,7 @@ __device__ __forceinline__ void tile_compute_store(const PassParams& p, long lon
       C v = F::from_s(sm[c * cs + pidx(r, sh)]);
       if (p.do_scale) v = apply_scale<F>(v, p);
       gstore<F, OUT>(dst, p.out_off[k], v);
+      if (p.spec_kind) spec_store<F>(p, tb + p.out_off[k], v);
     }
     return;
   }
@@ -510,6 +534,13 @@ __device__ __forceinline__ const typename IOElem<IN>::T* col_src(const PassParam
   return reinterpret_cast<const IE*>(p.in_ptrs[line]) + j * p.s;
 }
 
+// Linear-layout index (IO elements from p.out) of row 0 of output column c.
+__device__ __forceinline__ long long col_index_out(const PassParams& p, long long line0,
+                                                   long long j0, int c) {
+  const long long jd0 = ((j0 >> p.logNs) << (p.logNs + p.logR)) + (j0 & (p.Ns - 1));
+  return line_base(p, line0) + jd0 * p.s + col_off_out(p, c);
+}
+
 template <int OUT>
 __device__ __forceinline__ typename IOElem<OUT>::T* col_dst(const PassParams& p, long long line0,
                                                            long long j0, int c) {
@@ -633,6 +664,15 @@ __device__ __forceinline__ void last_subpass(const PassParams& p, long long line
       if (p.do_scale) w = apply_scale<F>(w, p);
       gstore<F, OUT>(dst, t * step, w);
     }
+    if (p.spec_kind) {
+      const long long i0 = col_index_out(p, line0, j0, c) + j * rs;
+#pragma unroll
+      for (int t = 0; t < Q; ++t) {
+        C w = v[t];
+        if (p.do_scale) w = apply_scale<F>(w, p);
+        spec_store<F>(p, i0 + t * step, w);
+      }
+    }
   }
 }
 
@@ -683,6 +723,7 @@ __device__ __forceinline__ void only_subpass(const PassParams& p, long long line
       C w = v[t];
       if (p.do_scale) w = apply_scale<F>(w, p);
       gstore<F, OUT>(dst, t * rs_out, w);
+      if (p.spec_kind) spec_store<F>(p, col_index_out(p, line0, j0, c) + t * rs_out, w);
     }
   }
 }
@@ -826,6 +867,11 @@ __device__ __forceinline__ void last_subpass16_tc(const PassParams& p, long long
       }
       gstore<F32, OUT>(dst, g * step, y0);
       gstore<F32, OUT>(dst, (g + 8) * step, y1);
+      if (p.spec_kind) {
+        const long long i0 = col_index_out(p, line0, j0, co) + jo * rs;
+        spec_store<F32>(p, i0 + g * step, y0);
+        spec_store<F32>(p, i0 + (g + 8) * step, y1);
+      }
     }
   }
 }
@@ -992,10 +1038,190 @@ cudaError_t dispatch_io(IOType in, IOType out, const PassParams& p, int threads,
   return cudaErrorInvalidValue;
 }
 
+// ---------------------------------------------------------------------------
+// realft twist fused into a pass (src/Real_FT.rs:24-46 forward, :120-142
+// inverse, restated 0-based; the same arithmetic as k_realft_twist): the
+// forward twist is applied by the last pass of the n/2-point forward FFT as it
+// stores, the inverse twist by the first pass of the inverse FFT after it
+// loads.  Output k of a line of L = n/2 points combines Z_k with Z_{L-k}, so a
+// tile holds both: in a multi-pass schedule a "mirror tile" owns columns j and
+// NC - j (NC = L/R columns per line); single-pass tiles hold whole lines.
+// The input and output element types are dispatched at run time, so one
+// kernel per form, direction and thread count serves every IO combination.
+// ---------------------------------------------------------------------------
+// Column of tile column c of mirror tile tl (tiles of C = 2^logC columns):
+// the first C/2 columns are tl*C/2 + c, the second C/2 their mirrors NC - j
+// in ascending order, with column NC/2 (its own mirror) standing in for the
+// mirror of column 0.  Over the NC/C tiles every column appears once.
+__device__ __forceinline__ long long mirror_col(long long tl, int c, int logC, long long NC) {
+  const int half = 1 << (logC - 1);
+  if (c < half) return tl * half + c;
+  const long long j = NC - (tl + 1) * half + 1 + (c - half);
+  return j == NC ? (NC >> 1) : j;
+}
+
+// Tile position (c2, r2) of the element paired with (c, r): index
+// k = j + r NC of the line pairs with L - k = (NC - j) + (R - 1 - r) NC.
+__device__ __forceinline__ void mirror_partner(long long tl, int c, int r, int logC, int logR,
+                                               int& c2, int& r2) {
+  const int Cn = 1 << logC, R = 1 << logR;
+  if (tl == 0 && c == 0) { c2 = 0; r2 = (R - r) & (R - 1); }        // column 0
+  else if (tl == 0 && c == Cn - 1) { c2 = Cn - 1; r2 = R - 1 - r; }  // column NC/2
+  else { c2 = Cn - 1 - c; r2 = R - 1 - r; }
+}
+
+// Twisted value of slot k (0 < k < L) from Z_k (own) and Z_{L-k} (part):
+// h1 = (Z_k + conj Z_{L-k})/2, h2 = -IS i (Z_k - conj Z_{L-k})/2, result
+// h1 + w^k h2 with w = exp(IS 2 pi i / n), 2^logn = n.  Slot 0 packs DC and
+// Nyquist: (h + v, h - v) forward, half that inverse.  Slot L/2 pairs with
+// itself and comes out unchanged.
+template <class F, int IS>
+__device__ __forceinline__ typename F::C twist_elem(typename F::C own, typename F::C part,
+                                                    long long k, int logn, const Twiddles& tw) {
+  using C = typename F::C;
+  if (k == 0) {
+    const C s = F::add(C{own.x, own.x}, F::conj(C{own.y, own.y}));
+    return IS > 0 ? s : F::scale(s, 0.5);
+  }
+  const C cp = F::conj(part);
+  const C h1 = F::scale(F::add(own, cp), 0.5);
+  const C h2 = F::scale(F::mul_j(F::sub(own, cp), -IS), 0.5);
+  return F::add(h1, F::mul(h2, twiddle<F>(tw, logn, (unsigned)k, IS)));
+}
+
+template <class F>
+__device__ __forceinline__ typename F::C gload_rt(int io, const void* p, long long i) {
+  if (io == IO_D2) return gload<F, IO_D2>(p, i);
+  if (io == IO_F2) return gload<F, IO_F2>(p, i);
+  return gload<F, IO_F4>(p, i);
+}
+template <class F>
+__device__ __forceinline__ void gstore_rt(int io, void* p, long long i, typename F::C v) {
+  if (io == IO_D2) gstore<F, IO_D2>(p, i, v);
+  else if (io == IO_F2) gstore<F, IO_F2>(p, i, v);
+  else gstore<F, IO_F4>(p, i, v);
+}
+
+// One tile per CTA, staged.  SG > 0: the forward FFT's last pass with the
+// forward twist on its stores; SG < 0: the inverse FFT's first pass with the
+// inverse twist on its loaded tile.  Lines are linear (no pointer tables).
+template <class F, int SG, int T>
+__global__ void __launch_bounds__(T) k_twist_pass(PassParams p, int in_io, int out_io) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using C = typename F::C;
+  typename F::S* sm = reinterpret_cast<typename F::S*>(smem_raw);
+  constexpr int sh = F::kPadShift;
+  const int tid = threadIdx.x;
+  const int logR = p.logR, logC = p.logC;
+  const int R = 1 << logR, Cn = 1 << logC;
+  const int cs = col_stride(logR, sh);
+  const int logn = p.logL + 1;  // n = 2L reals
+  long long line0, j0;
+  tile_origin(p, blockIdx.x, line0, j0);
+  const bool mir = p.mode == 0;  // multi-pass: mirror tiles; else whole lines
+  const long long NC = p.L >> logR;
+  const long long tl = mir ? (j0 >> logC) : 0;
+  // 1. load the tile (all loads first), inter-pass twiddles, stage
+  {
+    C v[kEPT];
+#pragma unroll
+    for (int k = 0; k < kEPT; ++k) {
+      int c, r;
+      elem_cr(tid + k * T, p.in_rcontig, logR, logC, c, r);
+      const long long line = mir ? line0 : line0 + c;
+      const long long j = mir ? mirror_col(tl, c, logC, NC) : j0;
+      v[k] = (line < p.nlines)
+                 ? gload_rt<F>(in_io, p.in, line_base(p, line) + (j + (long long)r * NC) * p.s)
+                 : F::from_d(0.0, 0.0);
+    }
+#pragma unroll
+    for (int k = 0; k < kEPT; ++k) {
+      int c, r;
+      elem_cr(tid + k * T, p.in_rcontig, logR, logC, c, r);
+      if (p.logNs > 0) {
+        const long long j = mir ? mirror_col(tl, c, logC, NC) : j0;
+        const unsigned jm = (unsigned)(j & (p.Ns - 1));
+        if (jm != 0 && r != 0)
+          v[k] = F::mul(v[k], twiddle<F>(p.tw, p.logNs + logR, jm * (unsigned)r, SG));
+      }
+      sm[c * cs + pidx(r, sh)] = F::to_s(v[k]);
+    }
+  }
+  __syncthreads();
+  // 2. inverse twist of the loaded tile (first pass of the inverse FFT)
+  if constexpr (SG < 0) {
+    C tv[kEPT];
+#pragma unroll
+    for (int k = 0; k < kEPT; ++k) {
+      const int e = tid + k * T;
+      const int c = e & (Cn - 1), r = e >> logC;
+      int c2 = c, r2 = (R - r) & (R - 1);
+      if (mir) mirror_partner(tl, c, r, logC, logR, c2, r2);
+      const long long kk = mir ? mirror_col(tl, c, logC, NC) + (long long)r * NC : r;
+      tv[k] = twist_elem<F, -1>(F::from_s(sm[c * cs + pidx(r, sh)]),
+                                F::from_s(sm[c2 * cs + pidx(r2, sh)]), kk, logn, p.tw);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kEPT; ++k) {
+      const int e = tid + k * T;
+      sm[(e & (Cn - 1)) * cs + pidx(e >> logC, sh)] = F::to_s(tv[k]);
+    }
+    __syncthreads();
+  }
+  // 3. the R-point DFTs of the columns
+  run_subpasses<F, SG, T>(p, sm, cs, tid);
+  // 4. store at the autosorted positions (forward twist in the last pass)
+#pragma unroll 4
+  for (int k = 0; k < kEPT; ++k) {
+    int c, r;
+    elem_cr(tid + k * T, p.out_rcontig, logR, logC, c, r);
+    const long long line = mir ? line0 : line0 + c;
+    if (line >= p.nlines) continue;
+    const long long j = mir ? mirror_col(tl, c, logC, NC) : j0;
+    const long long jd = ((j >> p.logNs) << (p.logNs + logR)) + (j & (p.Ns - 1));
+    C v = F::from_s(sm[c * cs + pidx(r, sh)]);
+    if constexpr (SG > 0) {
+      int c2 = c, r2 = (R - r) & (R - 1);
+      if (mir) mirror_partner(tl, c, r, logC, logR, c2, r2);
+      v = twist_elem<F, 1>(v, F::from_s(sm[c2 * cs + pidx(r2, sh)]), jd + (long long)r * p.Ns,
+                           logn, p.tw);
+    }
+    if (p.do_scale) v = apply_scale<F>(v, p);
+    gstore_rt<F>(out_io, p.out, line_base(p, line) + (jd + (long long)r * p.Ns) * p.s, v);
+  }
+}
+
+template <class F, int SG, int T>
+inline cudaError_t launch_twist_one(IOType in, IOType out, const PassParams& p, cudaStream_t st) {
+  static DeviceOnce attr_done;
+  const size_t smem = pass_smem_bytes<F>(T);
+  cudaError_t e = smem_opt_in(k_twist_pass<F, SG, T>, smem, attr_done);
+  if (e != cudaSuccess) return e;
+  if (p.tiles <= 0 || p.tiles > 0x7FFFFFFFll) return cudaErrorInvalidValue;
+  k_twist_pass<F, SG, T><<<dim3((unsigned)p.tiles), T, smem, st>>>(p, (int)in, (int)out);
+  return cudaGetLastError();
+}
+
+template <class F, int SG>
+cudaError_t dispatch_twist(IOType in, IOType out, const PassParams& p, int threads,
+                           cudaStream_t st) {
+  switch (threads) {
+    case 256: return launch_twist_one<F, SG, 256>(in, out, p, st);
+    case 128: return launch_twist_one<F, SG, 128>(in, out, p, st);
+    case 64: return launch_twist_one<F, SG, 64>(in, out, p, st);
+    default: return launch_twist_one<F, SG, 32>(in, out, p, st);
+  }
+}
+
 #define GBFFT_DECLARE_DISPATCH(FORM)                                                          \
   extern template cudaError_t dispatch_io<FORM, 1>(IOType, IOType, const PassParams&, int,    \
                                                    cudaStream_t);                             \
   extern template cudaError_t dispatch_io<FORM, -1>(IOType, IOType, const PassParams&, int,   \
-                                                    cudaStream_t);
+                                                    cudaStream_t);                            \
+  extern template cudaError_t dispatch_twist<FORM, 1>(IOType, IOType, const PassParams&, int, \
+                                                      cudaStream_t);                          \
+  extern template cudaError_t dispatch_twist<FORM, -1>(IOType, IOType, const PassParams&, int, \
+                                                       cudaStream_t);
 
 }  // namespace gbfft

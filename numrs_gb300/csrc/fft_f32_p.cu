@@ -4,4 +4,6 @@
 namespace gbfft {
 template cudaError_t dispatch_io<F32, 1>(IOType, IOType, const PassParams&, int,
                                           cudaStream_t);
+template cudaError_t dispatch_twist<F32, 1>(IOType, IOType, const PassParams&, int,
+                                            cudaStream_t);
 }  // namespace gbfft

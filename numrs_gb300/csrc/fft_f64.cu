@@ -5,4 +5,8 @@
 namespace gbfft {
 template cudaError_t dispatch_io<F64, 1>(IOType, IOType, const PassParams&, int, cudaStream_t);
 template cudaError_t dispatch_io<F64, -1>(IOType, IOType, const PassParams&, int, cudaStream_t);
+template cudaError_t dispatch_twist<F64, 1>(IOType, IOType, const PassParams&, int,
+                                            cudaStream_t);
+template cudaError_t dispatch_twist<F64, -1>(IOType, IOType, const PassParams&, int,
+                                            cudaStream_t);
 }  // namespace gbfft

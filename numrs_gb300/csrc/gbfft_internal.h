@@ -73,6 +73,16 @@ struct PassParams {
   double scale;
   float fscale;     // scale as a float for the FP32-pipe forms (set at launch)
   long long tiles;  // grid size
+  // Spectrum epilogue (last pass of a transform, linear layouts only): beside
+  // the complex output element i, spec[i] = |X| (spec_kind 1) or |X|^2
+  // (spec_kind 2); 0 = off.
+  double* spec;
+  int spec_kind;
+  // realft twist fused into this pass (src/Real_FT.rs:24-46,120-142):
+  // +1 = forward twist after the last pass of the forward FFT, -1 = inverse
+  // twist before the first pass of the inverse FFT; 0 = none.  Lines have
+  // L = n/2 points; the pass runs as k_twist_pass.
+  int twist;
   // Per-slot parts of the global element indices of a tile, for layouts
   // without per-line pointer tables: slot k of thread tid holds tile element
   // e = tid + k*T, and its index is a per-thread base plus in_off[k] (load
@@ -166,6 +176,13 @@ cudaError_t launch_correl_direct(const double* a, const double* b, double* out, 
 cudaError_t launch_twofft_pack(const double* d1, const double* d2, double* fft1, long long n,
                                cudaStream_t st);
 cudaError_t launch_twofft_split(double* fft1, double* fft2, long long n, cudaStream_t st);
+// twofft-packed convlv/correl: z = a + i b (m > 0: b is an m-tap response,
+// expanded in wrap-around order), then after the n-point FFT the fused split,
+// product and inverse twist in place (kind as launch_spectral_product).
+cudaError_t launch_pack_pair(const double* a, const double* b, long long m, double* z, long long n,
+                             cudaStream_t st);
+cudaError_t launch_spectral_two(Form f, int kind, double* z, long long n, Twiddles tw,
+                                cudaStream_t st);
 // rlft3 steps: speq gather (forward) and the twist along the last axis.
 cudaError_t launch_rlft3_speq(const double* data, double* speq, long long nn1, long long nn2,
                               long long nn3, cudaStream_t st);

@@ -72,6 +72,9 @@ struct Ctx {
   long long alloc_calls = 0;
   unsigned int dbg_spin_limit = 0;
   unsigned int dbg_need_extra = 0;
+  // convlv/correl forward transforms: 0 = the two inputs as two n/2-point
+  // realft lines, 1 = packed as one n-point complex FFT (twofft)
+  int spectral_path = 0;
 };
 
 Ctx g;
@@ -365,7 +368,10 @@ int launch_pass(Form f, int sign, IOType in, IOType out, const PassParams& p, in
 }
 
 // Run an axis plan on `data` (interleaved double complex, device memory).
-int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale = 1.0) {
+// spec/spec_kind: optional spectrum epilogue of the last pass (see PassParams).
+// twist: realft twist fused into the last (+1) or first (-1) pass.
+int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale = 1.0,
+             double* spec = nullptr, int spec_kind = 0, int twist = 0) {
   Twiddles tw;
   TRY(tables(f, tw));
   const IOType sio = scratch_io(f);
@@ -398,32 +404,54 @@ int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale = 1.
       p.do_scale = 1;
       p.scale = scale;
     }
+    if (last && spec_kind) {
+      p.spec = spec;
+      p.spec_kind = spec_kind;
+    }
+    if ((twist > 0 && last) || (twist < 0 && first)) p.twist = twist;
     TRY(launch_pass(f, sign, in_t, out_t, p, ps.threads));
   }
   return GBFFT_OK;
 }
 
-// Out-of-place run of a one- or two-pass plan: the first pass reads `in` (or
-// the per-line pointers `in_lines`, a device array), the last pass writes
-// `out`.  Either may be host memory when g.host_direct is set.
+// Whether the realft twist can ride on the plan's last (twist > 0) or first
+// (twist < 0) pass: a multi-pass plan's mirror tiles need at least two
+// columns; a single-pass plan's tiles hold whole lines.
+bool twist_fits(const AxisPlan& ap, int twist) {
+  if (ap.passes.empty()) return false;
+  const PassParams& p = (twist > 0 ? ap.passes.back() : ap.passes.front()).p;
+  if (p.s != 1) return false;
+  if (p.mode == 0) return p.logC >= 1 && (p.L >> p.logR) >= (1ll << p.logC);
+  return ap.passes.size() == 1;
+}
+
+// Out-of-place run of a plan: the first pass reads `in` (or the per-line
+// pointers `in_lines`, a device array), the last pass writes `out`; the passes
+// between ping-pong through device scratch (two halves for three or more
+// passes).  `in` and `out` may be host memory when g.host_direct is set: the
+// link traffic then overlaps the first and last passes' arithmetic instead of
+// preceding and following the transform as staging copies.
 int run_axis_io(Form f, int sign, const AxisPlan& ap, const void* in,
-                const void* const* in_lines, void* out) {
+                const void* const* in_lines, void* out, double* spec = nullptr,
+                int spec_kind = 0) {
   Twiddles tw;
   TRY(tables(f, tw));
   const IOType sio = scratch_io(f);
   const size_t P = ap.passes.size();
-  if (P > 2) {
-    // in-place passes through a device copy when the plan is longer
-    return fail(GBFFT_UNSUPPORTED_SIZE, "run_axis_io: %zu passes", P);
-  }
-  if (P == 2) TRY(ensure(g.scratch, ap.scratch_elems * io_bytes(sio)));
+  const size_t half = ap.scratch_elems * io_bytes(sio);
+  if (P >= 2) TRY(ensure(g.scratch, half * (P >= 3 ? 2 : 1)));
+  void* sbuf[2] = {g.scratch.p, P >= 3 ? (void*)((char*)g.scratch.p + half) : g.scratch.p};
   for (size_t i = 0; i < P; ++i) {
     PassParams p = ap.passes[i].p;
     p.tw = tw;
     const bool first = i == 0, last = i + 1 == P;
-    p.in = first ? in : g.scratch.p;
+    p.in = first ? in : sbuf[(i - 1) & 1];
     p.in_ptrs = first ? in_lines : nullptr;
-    p.out = last ? out : g.scratch.p;
+    p.out = last ? out : sbuf[i & 1];
+    if (last && spec_kind) {
+      p.spec = spec;
+      p.spec_kind = spec_kind;
+    }
     TRY(launch_pass(f, sign, first ? IO_D2 : sio, last ? IO_D2 : sio, p, ap.passes[i].threads));
   }
   return GBFFT_OK;
@@ -452,8 +480,6 @@ void tune_load() {
     g_tuned[std::make_tuple(L, s, nl, lq, ls, f)] = tl;
   fclose(fp);
 }
-
-int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale);
 
 int tune_tile(Form f, long long L, long long s, long long nlines, int lq_log, long long lstride) {
   const size_t span = (s == 1) ? (size_t)((nlines - 1) * lstride + L) : (size_t)(nlines * L);
@@ -638,6 +664,12 @@ int realft_dev(Form f, double* d, long long n, int isign, long long batch = 1,
   Twiddles tw;
   TRY(tables(f, tw));
   const long long nh = n / 2;
+  if (nh >= 2) {
+    // the twist rides on the last pass of the forward FFT or the first pass
+    // of the inverse one: no pass of its own over the data
+    const AxisPlan& ap = axis_plan(nh, 1, batch, 0, dist / 2, f);
+    if (twist_fits(ap, isign)) return run_axis(f, isign, ap, d, 1.0, nullptr, 0, isign);
+  }
   if (isign == 1) {
     TRY(fft_lines(f, 1, d, nh, batch, dist / 2));
     {
@@ -932,14 +964,19 @@ int spectral_direct(Form f, int kind, const double* a, const double* b, long lon
   return GBFFT_OK;
 }
 
-// Whether the plan of `nlines` lines of L points can run with host arrays read
-// and written by its first and last passes (at most two passes).
-// Whether run_axis_io can take the axis (at most two passes).
+// Whether run_axis_io takes the plan of `nlines` lines of L points, with the
+// first pass reading through a per-line pointer table (pass counts of one or
+// two; the pointer-table layouts are used only by the convolution paths).
 bool io_fits(long long L, long long nlines, Form f) {
   return L <= (1ll << kBatchMaxLog) && axis_plan(L, 1, nlines, 0, L, f).passes.size() <= 2;
 }
+// Whether a linear host array of `nlines` lines of L points can be read and
+// written by the plan's first and last passes directly (any pass count).
 bool direct_fits(long long L, long long nlines, Form f) {
-  return g.host_direct && io_fits(L, nlines, f);
+  (void)L;
+  (void)nlines;
+  (void)f;
+  return g.host_direct;
 }
 
 }  // namespace
@@ -1029,6 +1066,13 @@ int gbfft_profile_read(int kind, double* ms, long long* launches, double* bytes,
   return GBFFT_OK;
 }
 
+int gbfft_set_spectral_path(int path) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (path != 0 && path != 1) return fail(GBFFT_INVALID_ARG, "spectral path must be 0 or 1");
+  g.spectral_path = path;
+  return GBFFT_OK;
+}
+
 int gbfft_debug_set(int key, long long value) {
   std::lock_guard<std::mutex> lk(g_mu);
   switch (key) {
@@ -1078,6 +1122,52 @@ int gbfft_four1(double* data, size_t nn, int isign, const gbfft_opts* opts) {
   TRY(stage_inout(c, g.stage_a, data, 2 * nn, &d));
   TRY(fft_lines(c.form(), isign, d, (long long)nn, 1, (long long)nn));
   TRY(unstage(c, data, d, 2 * nn));
+  return ss.finish(c);
+}
+
+// FFTProcessor::fft followed by magnitude_spectrum / power_spectrum
+// (src/FFT_1.rs:166,206,218) with the spectrum written by the transform's
+// last pass, from the values it stores: no separate pass over the spectrum.
+int gbfft_four1_spectrum(double* data, size_t nn, int isign, int kind, double* spec,
+                         const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  if (!data || !spec) return fail(GBFFT_INVALID_ARG, "four1_spectrum: null pointer");
+  TRY(dev_aligned(c, "four1_spectrum", {data}));
+  TRY(check_isign(isign));
+  if (kind != 0 && kind != 1)
+    return fail(GBFFT_INVALID_ARG, "four1_spectrum: kind must be 0 (magnitude) or 1 (power)");
+  if (!is_pow2(nn) || ilog2(nn) > kMaxAxisLog)
+    return fail(GBFFT_UNSUPPORTED_SIZE, "four1_spectrum: nn=%zu must be a power of two <= 2^%d",
+                nn, kMaxAxisLog);
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  const int sk = kind == 0 ? 1 : 2;
+  const Form f = c.form();
+  if (!c.dev() && nn > 1 && al16(data) && direct_fits((long long)nn, 1, f)) {
+    // the first pass reads the caller's array, the last pass writes it and
+    // the spectrum straight into host memory
+    TRY(run_axis_io(f, isign, axis_plan((long long)nn, 1, 1, 0, (long long)nn, f), data, nullptr,
+                    data, spec, sk));
+    return ss.finish(c);
+  }
+  double* d;
+  TRY(stage_inout(c, g.stage_a, data, 2 * nn, &d));
+  double* sp = spec;
+  if (!c.dev()) {
+    TRY(ensure(g.stage_b, nn * sizeof(double)));
+    sp = (double*)g.stage_b.p;
+  }
+  if (nn == 1) {
+    // the 1-point transform is the identity
+    CK(launch_spectrum(kind, d, sp, 1, g.cur));
+    g.launches++;
+  } else {
+    TRY(run_axis(f, isign, axis_plan((long long)nn, 1, 1, 0, (long long)nn, f), d, 1.0, sp, sk));
+  }
+  TRY(unstage(c, data, d, 2 * nn));
+  if (!c.dev()) TRY(d2h(spec, sp, nn * sizeof(double)));
   return ss.finish(c);
 }
 
@@ -1288,10 +1378,55 @@ static int load_one(const Call& c, double* dst, const double* src, size_t double
   return c.dev() ? d2d(dst, src, doubles * sizeof(double)) : h2d(dst, src, doubles * sizeof(double));
 }
 
+// The twofft-packed form of convlv/correl (n >= 4): the inputs become the
+// real and imaginary parts of one n-point complex FFT (the pack kernel reads
+// the caller's arrays and expands the response), one kernel splits the two
+// spectra, multiplies them and applies the inverse realft twist in place, and
+// the inverse n/2-point FFT writes the answer.
+static int spectral_twofft(const Call& c, int kind, const double* a, const double* b, size_t n,
+                           size_t m, double* ans) {
+  const Form f = c.form();
+  Twiddles tw;
+  TRY(tables(f, tw));
+  TRY(ensure(g.work, 2 * n * sizeof(double)));
+  double* z = (double*)g.work.p;
+  const double *da = a, *db = b;
+  const size_t mb = (kind == 2) ? n : m;  // doubles of the second input
+  if (!c.dev() && !g.host_direct) {
+    TRY(ensure(g.stage_c, (n + mb) * sizeof(double)));
+    double* in = (double*)g.stage_c.p;
+    TRY(h2d(in, a, n * sizeof(double)));
+    TRY(h2d(in + n, b, mb * sizeof(double)));
+    da = in;
+    db = in + n;
+  }
+  CK(launch_pack_pair(da, db, kind == 2 ? 0 : (long long)m, z, (long long)n, g.cur));
+  g.launches++;
+  TRY(run_axis(f, 1, axis_plan((long long)n, 1, 1, 0, (long long)n, f), z));
+  {
+    ProfScope ps(PK_SPECTRAL, 3.0 * n * 8);
+    CK(launch_spectral_two(f, kind, z, (long long)n, tw, g.cur));
+  }
+  g.launches++;
+  const long long nh = (long long)n / 2;
+  if (al16(ans) && (c.dev() || g.host_direct) && io_fits(nh, 1, f)) {
+    TRY(run_axis_io(f, -1, axis_plan(nh, 1, 1, 0, nh, f), z, nullptr, ans));
+    return GBFFT_OK;
+  }
+  TRY(run_axis(f, -1, axis_plan(nh, 1, 1, 0, nh, f), z));
+  if (c.dev()) TRY(d2d(ans, z, n * sizeof(double)));
+  else TRY(d2h(ans, z, n * sizeof(double)));
+  return GBFFT_OK;
+}
+
 static int spectral_call(const Call& c, int kind, const double* a, const double* b, size_t n,
                          size_t m, double* ans) {
   TRY(init_locked(g.device));
   StreamScope ss(c);
+  if (g.spectral_path == 1 && n >= 4 && !(kind == 2 && a == b)) {
+    TRY(spectral_twofft(c, kind, a, b, n, m, ans));
+    return ss.finish(c);
+  }
   if (kind == 2 && a == b) {
     // autocorrelation (src/Correlation.rs:281-286): one forward transform, its
     // spectrum used as both operands of the conjugate product

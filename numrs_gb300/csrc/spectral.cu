@@ -443,6 +443,101 @@ cudaError_t launch_twofft_pack(const double* d1, const double* d2v, double* fft1
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// twofft-packed convlv / correl (the fast path of src/FFT_2.rs:3-17 applied to
+// the two forward transforms of src/Convolve.rs:66-77 and
+// src/Correlation.rs:53-55): the two real inputs travel as the real and
+// imaginary parts of one n-point complex FFT.
+// ---------------------------------------------------------------------------
+// z_j = a_j + i b_j.  With m > 0, b is an m-tap response in wrap-around order
+// (Numerical Recipes convlv contract) expanded on the fly to n values.
+__global__ void k_pack_pair(const double* a, const double* b, long long m, double* z,
+                            long long n) {
+  const long long half = (m - 1) / 2;
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
+       j += (long long)gridDim.x * blockDim.x) {
+    double v;
+    if (m == 0) v = b[j];
+    else if (half > 0 && j >= n - half) v = b[m - (n - j)];
+    else if (j < (m + 1) / 2) v = b[j];
+    else v = 0.0;
+    reinterpret_cast<d2*>(z)[j] = d2{a[j], v};
+  }
+}
+
+cudaError_t launch_pack_pair(const double* a, const double* b, long long m, double* z, long long n,
+                             cudaStream_t st) {
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  k_pack_pair<<<blocks, 256, 0, st>>>(a, b, m, z, n);
+  return cudaGetLastError();
+}
+
+// Z is the n-point FFT (isign = +1) of a + i b.  The spectra of a and b are
+// A_k = (Z_k + conj Z_{n-k})/2 and B_k = -i (Z_k - conj Z_{n-k})/2.  For each
+// pair (k, n/2 - k) of the packed half spectrum: both products (scaled by
+// 2/n as k_spectral's), then the inverse realft twist -- the input of the
+// inverse n/2-point FFT, written over the first n/2 slots of Z.  Every slot
+// of Z is read by one thread only, the one that writes it, so the step runs
+// in place.
+template <class F, int KIND>
+__global__ void k_spectral_two(double* z, long long n, Twiddles tw) {
+  using C = typename F::C;
+  const long long nh = n / 2, nq = n / 4;
+  const double inv_no2 = 2.0 / (double)n;
+  const int logn = 63 - __clzll(n);
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k <= nq;
+       k += (long long)gridDim.x * blockDim.x) {
+    if (k == 0) {
+      // DC and Nyquist bins of A and B are real: Re/Im of Z_0 and Z_{n/2}
+      const double ad = z[0], bd = z[1];
+      const double an = (n > 1) ? z[2 * nh] : 0.0, bn = (n > 1) ? z[2 * nh + 1] : 0.0;
+      const double pd = spec_prod_real<F, KIND>(ad, bd, inv_no2);
+      const double pn = spec_prod_real<F, KIND>(an, bn, inv_no2);
+      z[0] = 0.5 * (pd + pn);
+      z[1] = 0.5 * (pd - pn);
+      continue;
+    }
+    if (k == nq) {
+      // middle slot n/4: the twists are the identity
+      const C zk = ldc<F>(z, k), zr = F::conj(ldc<F>(z, n - k));
+      const C a2 = F::add(zk, zr), b2 = F::mul_j(F::sub(zk, zr), -1);  // 2A, 2B
+      stc<F>(z, k, spec_prod<F, KIND>(a2, b2, (KIND == 1) ? inv_no2 : 0.25 * inv_no2, 2.0));
+      continue;
+    }
+    const long long m = nh - k;
+    const C zk = ldc<F>(z, k), zkr = F::conj(ldc<F>(z, n - k));
+    const C zm = ldc<F>(z, m), zmr = F::conj(ldc<F>(z, n - m));
+    const C ak = F::add(zk, zkr), bk = F::mul_j(F::sub(zk, zkr), -1);  // 2A_k, 2B_k
+    const C am = F::add(zm, zmr), bm = F::mul_j(F::sub(zm, zmr), -1);
+    const double sc = (KIND == 1) ? 0.5 * inv_no2 : 0.125 * inv_no2;
+    C pk = spec_prod<F, KIND>(ak, bk, sc, 2.0);
+    C pm = spec_prod<F, KIND>(am, bm, sc, 2.0);
+    twist2_pair<F, -1>(pk, pm, F::conj(twiddle<F>(tw, logn, k, 1)));
+    stc<F>(z, k, pk);
+    stc<F>(z, m, pm);
+  }
+}
+
+cudaError_t launch_spectral_two(Form f, int kind, double* z, long long n, Twiddles tw,
+                                cudaStream_t st) {
+  long long work = n / 4 + 1;
+  int blocks = (int)((work + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+#define SP2_LAUNCH(FT)                                                        \
+  switch (kind) {                                                             \
+    case 0: k_spectral_two<FT, 0><<<blocks, 256, 0, st>>>(z, n, tw); break;   \
+    case 1: k_spectral_two<FT, 1><<<blocks, 256, 0, st>>>(z, n, tw); break;   \
+    default: k_spectral_two<FT, 2><<<blocks, 256, 0, st>>>(z, n, tw); break;  \
+  }
+  if (f == FORM_F64) { SP2_LAUNCH(F64) }
+  else if (f == FORM_F32 || f == FORM_TC32) { SP2_LAUNCH(F32) }
+  else { SP2_LAUNCH(DF64) }
+#undef SP2_LAUNCH
+  return cudaGetLastError();
+}
+
 cudaError_t launch_twofft_split(double* fft1, double* fft2, long long n, cudaStream_t st) {
   long long work = n / 2 + 1;
   int blocks = (int)((work + 255) / 256);
