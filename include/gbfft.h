@@ -177,6 +177,18 @@ int gbfft_realft(double* data, size_t n, int isign, const gbfft_opts* opts);
 int gbfft_fourn(double* data, const size_t* nn, size_t nn_len, size_t ndim, int isign,
                 const gbfft_opts* opts);
 
+/* FourFS::fourfs: src/Four_FS.rs:55 `fourfs(&mut self, nn: &[usize], ndim, isign)`,
+ * the out-of-core N-D FFT (validate_inputs, src/Four_FS.rs:328-339, as fourn).
+ * data is HOST memory (it may be larger than the GPU's memory), row-major,
+ * interleaved complex, transformed in place; every pass reads and writes host
+ * memory directly over the CPU-GPU link, and the GPU holds only its twiddle
+ * tables.  work: host scratch of 16 bytes per complex element, or NULL for one
+ * allocated (pageable) for the call.  data and work start on 16-byte
+ * boundaries.  Needs a GPU that reaches pageable host memory through the host
+ * page tables (Grace-Blackwell); elsewhere GBFFT_UNSUPPORTED_SIZE. */
+int gbfft_fourfs(double* data, const size_t* nn, size_t nn_len, size_t ndim, int isign,
+                 double* work, const gbfft_opts* opts);
+
 /* rlft3: src/Real_FT3.rs:8 / rlft3_optimized :145
  * `(data: &mut [f64], speq: &mut [f64], nn1, nn2, nn3, isign)`.
  * data nn1*nn2*nn3 reals, speq nn1*2*nn2 doubles.  Inverse returns

@@ -35,7 +35,7 @@ __all__ = [
     "autocorrel", "magnitude_spectrum", "power_spectrum", "real_to_complex",
     "complex_to_real", "ConvlvError", "CorrelError", "GbfftError", "launch_count",
     "FFTBatch", "four1_many", "set_async", "profile", "profile_read", "four1_noalloc",
-    "four1_spectrum", "set_spectral_path",
+    "four1_spectrum", "set_spectral_path", "fourfs",
     "correl_normalized", "correl_normalized_fast", "autocorrel_fast", "ConvlvProcessor",
     "RealFTProcessor", "TwoFFTProcessor",
 ]
@@ -309,6 +309,26 @@ def fourn(data, nn, ndim, isign, form="fp64"):
     arr = (ctypes.c_size_t * max(len(nn), 1))(*nn)
     o = _opts([a], form)
     st = _lib.load().gbfft_fourn(a.ptr, arr, len(nn), ndim, isign, ctypes.byref(o))
+    if st == _lib.INVALID_ARG:
+        raise ValueError(_lib.last_error())
+    _check(st)
+
+
+def fourfs(data, nn, ndim, isign, work=None, form="fp64"):
+    """Out-of-core N-D FFT (``FourFS::fourfs``, src/Four_FS.rs:55): ``data`` is
+    a host float64 array (it may be larger than the GPU's memory) transformed
+    in place; every pass reads and writes host memory over the CPU-GPU link.
+    ``work``: optional host scratch holding at least len(data) doubles (16
+    bytes per complex element); None allocates one for the call."""
+    a = _Arg(data, True)
+    if a.dev:
+        raise ValueError("fourfs works on host arrays (fourn takes device tensors)")
+    nn = list(nn)
+    arr = (ctypes.c_size_t * max(len(nn), 1))(*nn)
+    w = None if work is None else _Arg(work, True)
+    o = _opts([a], form)
+    st = _lib.load().gbfft_fourfs(a.ptr, arr, len(nn), ndim, isign, None if w is None else w.ptr,
+                                  ctypes.byref(o))
     if st == _lib.INVALID_ARG:
         raise ValueError(_lib.last_error())
     _check(st)

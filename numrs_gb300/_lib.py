@@ -44,6 +44,7 @@ SIGNATURES = {
     "gbfft_twofft": [_vp, _vp, _vp, _vp, _sz, _op],
     "gbfft_realft": [_vp, _sz, ctypes.c_int, _op],
     "gbfft_fourn": [_vp, ctypes.POINTER(_sz), _sz, _sz, ctypes.c_int, _op],
+    "gbfft_fourfs": [_vp, ctypes.POINTER(_sz), _sz, _sz, ctypes.c_int, _vp, _op],
     "gbfft_rlft3": [_vp, _vp, _sz, _sz, _sz, ctypes.c_int, _op],
     "gbfft_sinft": [_vp, _sz, _op],
     "gbfft_cosft1": [_vp, _sz, _op],

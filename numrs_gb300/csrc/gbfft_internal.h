@@ -18,23 +18,31 @@ enum IOType : int { IO_D2 = 0, IO_F2 = 1, IO_F4 = 2 };
 
 inline size_t io_bytes(IOType t) { return t == IO_F2 ? 8 : 16; }
 
-// Twiddle tables of one form.  dense holds levels S = 2^1 .. 2^kDenseLog
+// Twiddle tables of one form.  dense holds levels S = 2^1 .. 2^dense_log
 // back to back, entry S+e = exp(+2 pi i e / S).  partial holds, for each
-// level S = 2^(kDenseLog+1) .. 2^kMaxLog, the first kPartial entries of that
+// level S = 2^(dense_log+1) .. 2^kMaxLog, the first kPartial entries of that
 // level; a twiddle of a larger level is the product of one dense entry of
-// level S/kPartial and one partial entry.
-constexpr int kDenseLog = 16;
+// level S/kPartial and one partial entry (two loads and one complex product
+// instead of one load).  The library's tables are dense up to 2^kDenseLog
+// (2^20: every twiddle of an axis of up to 2^20 points is one load); the
+// no-allocation entry point keeps its fixed tables at the smaller
+// kDenseLogMin.
+constexpr int kDenseLog = 20;
+constexpr int kDenseLogMin = 16;
 constexpr int kPartialLog = 12;
 constexpr int kPartial = 1 << kPartialLog;
-constexpr int kMaxLog = kDenseLog + kPartialLog;  // 2^28 points per axis
-constexpr size_t kDenseEntries = size_t(2) << kDenseLog;
-constexpr size_t kPartialEntries = size_t(kMaxLog - kDenseLog) * kPartial;
+constexpr int kMaxLog = kDenseLogMin + kPartialLog;  // 2^28 points per axis
+__host__ __device__ constexpr size_t dense_entries(int dense_log) { return size_t(2) << dense_log; }
+__host__ __device__ constexpr size_t partial_entries(int dense_log) {
+  return size_t(kMaxLog - dense_log) * kPartial;
+}
 
 constexpr int kTileEPT = 16;  // complex elements per thread per tile
 
 struct Twiddles {
   const void* dense = nullptr;
   const void* partial = nullptr;
+  int dense_log = kDenseLog;  // largest level held densely
 };
 
 // One Stockham pass over an axis.  The axis has length L and stride s
@@ -141,7 +149,7 @@ cudaError_t launch_pass_df64(int sign, IOType in, IOType out, const PassParams& 
                              cudaStream_t st);
 cudaError_t launch_pass_tc32(int sign, IOType in, IOType out, const PassParams& p, int threads,
                              cudaStream_t st);
-cudaError_t launch_twiddles(Form f, void* dense, void* partial, cudaStream_t st);
+cudaError_t launch_twiddles(Form f, void* dense, void* partial, int dense_log, cudaStream_t st);
 
 // spectral / real-transform kernels (spectral.cu)
 struct SpecArgs {

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -180,20 +181,21 @@ int tables(Form f, Twiddles& tw) {
     size_t esz = (f == FORM_F32) ? 8 : 16;
     void* dense = nullptr;
     void* part = nullptr;
-    cudaError_t e = dev_alloc(&dense, kDenseEntries * esz);
-    if (e == cudaSuccess) e = dev_alloc(&part, kPartialEntries * esz);
+    cudaError_t e = dev_alloc(&dense, dense_entries(kDenseLog) * esz);
+    if (e == cudaSuccess) e = dev_alloc(&part, partial_entries(kDenseLog) * esz);
     if (e != cudaSuccess) {
       if (dense) cudaFree(dense);
       return fail(e == cudaErrorMemoryAllocation ? GBFFT_OOM : GBFFT_CUDA_ERROR,
                   "twiddle tables: cudaMalloc failed: %s", cudaGetErrorString(e));
     }
-    CK(launch_twiddles(f, dense, part, g.cur));
+    CK(launch_twiddles(f, dense, part, kDenseLog, g.cur));
     g.launches++;
     g.tw_dense[f] = dense;
     g.tw_part[f] = part;
   }
   tw.dense = g.tw_dense[f];
   tw.partial = g.tw_part[f];
+  tw.dense_log = kDenseLog;
   return GBFFT_OK;
 }
 
@@ -370,8 +372,11 @@ int launch_pass(Form f, int sign, IOType in, IOType out, const PassParams& p, in
 // Run an axis plan on `data` (interleaved double complex, device memory).
 // spec/spec_kind: optional spectrum epilogue of the last pass (see PassParams).
 // twist: realft twist fused into the last (+1) or first (-1) pass.
+// ext_scratch: scratch supplied by the caller (at least 16 bytes per complex
+// element of the axis' span) instead of the library's device scratch.
 int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale = 1.0,
-             double* spec = nullptr, int spec_kind = 0, int twist = 0) {
+             double* spec = nullptr, int spec_kind = 0, int twist = 0,
+             void* ext_scratch = nullptr) {
   Twiddles tw;
   TRY(tables(f, tw));
   const IOType sio = scratch_io(f);
@@ -381,8 +386,12 @@ int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale = 1.
   // first pass reads and only the last pass writes the caller's array.
   const bool two = sio == IO_F2 && P >= 3;
   const size_t half = ap.scratch_elems * io_bytes(sio);
-  if (ap.scratch_elems) TRY(ensure(g.scratch, half * (two ? 2 : 1)));
-  void* sbuf[2] = {g.scratch.p, two ? (void*)((char*)g.scratch.p + half) : g.scratch.p};
+  void* sb = ext_scratch;
+  if (!sb) {
+    if (ap.scratch_elems) TRY(ensure(g.scratch, half * (two ? 2 : 1)));
+    sb = g.scratch.p;
+  }
+  void* sbuf[2] = {sb, two ? (void*)((char*)sb + half) : sb};
   for (size_t i = 0; i < P; ++i) {
     const Pass& ps = ap.passes[i];
     const bool first = i == 0, last = i + 1 == P;
@@ -395,8 +404,8 @@ int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale = 1.
       in_t = first ? IO_D2 : sio;
       out_t = last ? IO_D2 : sio;
     } else {
-      p.in = ps.in_user ? data : g.scratch.p;
-      p.out = ps.out_user ? data : g.scratch.p;
+      p.in = ps.in_user ? data : sb;
+      p.out = ps.out_user ? data : sb;
       in_t = ps.in_user ? IO_D2 : sio;
       out_t = ps.out_user ? IO_D2 : sio;
     }
@@ -1335,6 +1344,71 @@ int gbfft_fourn(double* data, const size_t* nn, size_t nn_len, size_t ndim, int 
   TRY(stage_inout(c, g.stage_a, data, 2 * total, &d));
   TRY(fourn_dev(c.form(), d, dims, (int)ndim, isign));
   TRY(unstage(c, data, d, 2 * total));
+  return ss.finish(c);
+}
+
+// FourFS::fourfs (src/Four_FS.rs:55-73), the crate's out-of-core N-D FFT,
+// restated for a GPU that reaches host memory: the data stay in host memory
+// (they may exceed the GPU's memory), and every pass of every axis reads and
+// writes host memory directly over the CPU-GPU link, ping-ponging through a
+// host work array; the GPU holds only its twiddle tables.
+int gbfft_fourfs(double* data, const size_t* nn, size_t nn_len, size_t ndim, int isign,
+                 double* work, const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  // validate_inputs, src/Four_FS.rs:328-339
+  if (!nn || ndim == 0 || ndim > nn_len) return fail(GBFFT_INVALID_ARG, "fourfs: invalid dimensions");
+  if (isign != 1 && isign != -1) return fail(GBFFT_INVALID_ARG, "fourfs: isign must be 1 or -1");
+  for (size_t i = 0; i < ndim; ++i)
+    if (nn[i] <= 1) return fail(GBFFT_INVALID_ARG, "fourfs: invalid dimension size");
+  if (!data) return fail(GBFFT_INVALID_ARG, "fourfs: null data");
+  if (c.dev())
+    return fail(GBFFT_INVALID_ARG, "fourfs: data must be host memory (gbfft_fourn takes device data)");
+  if (!al16(data) || (work && !al16(work)))
+    return fail(GBFFT_INVALID_ARG, "fourfs: data and work must start on a 16-byte boundary");
+  long long dims[16];
+  if (ndim > 16) return fail(GBFFT_UNSUPPORTED_SIZE, "fourfs: ndim > 16");
+  size_t total = 1;
+  for (size_t i = 0; i < ndim; ++i) {
+    if (!is_pow2(nn[i]) || ilog2(nn[i]) > kMaxAxisLog)
+      return fail(GBFFT_UNSUPPORTED_SIZE, "fourfs: nn[%zu]=%zu must be a power of two", i, nn[i]);
+    dims[i] = (long long)nn[i];
+    total *= nn[i];
+  }
+  TRY(init_locked(g.device));
+  if (!g.host_direct)
+    return fail(GBFFT_UNSUPPORTED_SIZE,
+                "fourfs: this GPU does not reach pageable host memory directly (GBFFT_HOST_DIRECT=0 "
+                "or no host page-table access)");
+  StreamScope ss(c);
+  // the host work array: the caller's, or one allocated for this call
+  struct HostWork {
+    void* p = nullptr;
+    ~HostWork() {
+      if (p) {
+        cudaStreamSynchronize(g.cur);  // no pass may still read or write it
+        std::free(p);
+      }
+    }
+  } own;
+  void* ws = work;
+  if (!ws) {
+    const size_t bytes = ((total * 16 + 4095) / 4096) * 4096;
+    own.p = std::aligned_alloc(4096, bytes);
+    if (!own.p) return fail(GBFFT_OOM, "fourfs: host work allocation (%zu bytes) failed", bytes);
+    ws = own.p;
+  }
+  long long s = 1;
+  for (int dd = (int)ndim - 1; dd >= 0; --dd) {
+    const long long L = dims[dd];
+    const long long nl = (long long)total / L;
+    if (s == 1) TRY(run_axis(c.form(), isign, axis_plan(L, 1, nl, 0, L, c.form()), data, 1.0,
+                             nullptr, 0, 0, ws));
+    else TRY(run_axis(c.form(), isign, axis_plan(L, s, nl, ilog2((unsigned long long)s), L * s, c.form()),
+                      data, 1.0, nullptr, 0, 0, ws));
+    s *= L;
+  }
   return ss.finish(c);
 }
 

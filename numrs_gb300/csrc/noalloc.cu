@@ -40,8 +40,8 @@ constexpr int kNoAllocMaxLog = 20;
 // addresses; host code only ever passes the addresses that
 // cudaGetSymbolAddress returns for them.
 static __device__ __align__(256) d2 g_noalloc_scratch[size_t(1) << kNoAllocMaxLog];
-static __device__ __align__(256) d2 g_noalloc_tw_dense[kDenseEntries];
-static __device__ __align__(256) d2 g_noalloc_tw_partial[kPartialEntries];
+static __device__ __align__(256) d2 g_noalloc_tw_dense[dense_entries(kDenseLogMin)];
+static __device__ __align__(256) d2 g_noalloc_tw_partial[partial_entries(kDenseLogMin)];
 
 namespace {
 
@@ -57,14 +57,16 @@ struct NoAllocDevice {
 NoAllocDevice g_noalloc_dev[kMaxDevices];
 std::mutex g_noalloc_mu;
 
-// exp(+2 pi i e / S) for every dense and partial entry (same layout as the
-// library's FP64 tables).
+// exp(+2 pi i e / S) for every dense and partial entry (the layout of the
+// library's FP64 tables, dense up to 2^kDenseLogMin only so that the fixed
+// arrays stay small).
 __global__ void k_noalloc_twiddles(d2* dense, d2* partial) {
-  const size_t total = kDenseEntries + kPartialEntries;
+  constexpr size_t nd = dense_entries(kDenseLogMin);
+  const size_t total = nd + partial_entries(kDenseLogMin);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
     double c = 1.0, s = 0.0;
-    if (i < kDenseEntries) {
+    if (i < nd) {
       if (i >= 2) {
         const int logS = 63 - __clzll((long long)i);
         const long long S = 1ll << logS;
@@ -72,8 +74,8 @@ __global__ void k_noalloc_twiddles(d2* dense, d2* partial) {
       }
       dense[i] = d2{c, s};
     } else {
-      const size_t j = i - kDenseEntries;
-      const int lvl = (int)(j >> kPartialLog) + kDenseLog + 1;
+      const size_t j = i - nd;
+      const int lvl = (int)(j >> kPartialLog) + kDenseLogMin + 1;
       sincospi(2.0 * (double)(j & (kPartial - 1)) / (double)(1ll << lvl), &s, &c);
       partial[j] = d2{c, s};
     }
@@ -203,6 +205,7 @@ extern "C" int gbfft_four1_noalloc(double* data, size_t nn, int isign, void* str
   Twiddles tw;
   tw.dense = d->dense;
   tw.partial = d->partial;
+  tw.dense_log = kDenseLogMin;
   int logNs = 0;
   for (int i = 0; i < P; ++i) {
     PassParams p;

@@ -28,12 +28,13 @@ __device__ __forceinline__ void put_tw(typename F::TW* t, size_t i, double c, do
 }
 
 template <class F>
-__global__ void k_twiddles(typename F::TW* dense, typename F::TW* partial) {
-  const size_t total = kDenseEntries + kPartialEntries;
+__global__ void k_twiddles(typename F::TW* dense, typename F::TW* partial, int dense_log) {
+  const size_t nd = dense_entries(dense_log);
+  const size_t total = nd + partial_entries(dense_log);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
     double c, s;
-    if (i < kDenseEntries) {
+    if (i < nd) {
       // entry S + e of level S: S = highest power of two <= i
       if (i < 2) {
         c = 1.0; s = 0.0;
@@ -45,8 +46,8 @@ __global__ void k_twiddles(typename F::TW* dense, typename F::TW* partial) {
       }
       put_tw<F>(dense, i, c, s);
     } else {
-      size_t j = i - kDenseEntries;
-      int lvl = (int)(j >> kPartialLog) + kDenseLog + 1;
+      size_t j = i - nd;
+      int lvl = (int)(j >> kPartialLog) + dense_log + 1;
       long long e = (long long)(j & (kPartial - 1));
       sincospi(2.0 * (double)e / (double)(1ll << lvl), &s, &c);
       put_tw<F>(partial, j, c, s);
@@ -54,11 +55,11 @@ __global__ void k_twiddles(typename F::TW* dense, typename F::TW* partial) {
   }
 }
 
-cudaError_t launch_twiddles(Form f, void* dense, void* partial, cudaStream_t st) {
+cudaError_t launch_twiddles(Form f, void* dense, void* partial, int dense_log, cudaStream_t st) {
   dim3 g(1024), b(256);
-  if (f == FORM_F64) k_twiddles<F64><<<g, b, 0, st>>>((d2*)dense, (d2*)partial);
-  else if (f == FORM_F32) k_twiddles<F32><<<g, b, 0, st>>>((f2*)dense, (f2*)partial);
-  else k_twiddles<DF64><<<g, b, 0, st>>>((f4*)dense, (f4*)partial);
+  if (f == FORM_F64) k_twiddles<F64><<<g, b, 0, st>>>((d2*)dense, (d2*)partial, dense_log);
+  else if (f == FORM_F32) k_twiddles<F32><<<g, b, 0, st>>>((f2*)dense, (f2*)partial, dense_log);
+  else k_twiddles<DF64><<<g, b, 0, st>>>((f4*)dense, (f4*)partial, dense_log);
   return cudaGetLastError();
 }
 

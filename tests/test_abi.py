@@ -58,6 +58,13 @@ def test_argument_errors_need_no_gpu(lib):
     assert lib.gbfft_fourn(p, nn, 2, 2, 1, None) == L.INVALID_ARG
     assert lib.gbfft_fourn(p, nn, 2, 3, 1, None) == L.INVALID_ARG
     assert lib.gbfft_fourn(p, nn, 2, 1, 0, None) == L.INVALID_ARG
+    # fourfs validate_inputs, src/Four_FS.rs:328-339 (as the reference's
+    # test_invalid_inputs, src/Four_FS.rs:428-437)
+    one = (ctypes.c_size_t * 1)(1)
+    eight = (ctypes.c_size_t * 1)(8)
+    assert lib.gbfft_fourfs(p, one, 1, 1, 1, None, None) == L.INVALID_ARG
+    assert lib.gbfft_fourfs(p, eight, 1, 1, 0, None, None) == L.INVALID_ARG
+    assert lib.gbfft_fourfs(p, eight, 1, 2, 1, None, None) == L.INVALID_ARG
     # sizes and signs
     assert lib.gbfft_four1(p, 3, 1, None) == L.UNSUPPORTED_SIZE
     assert lib.gbfft_four1(p, 4, 2, None) == L.INVALID_ARG

@@ -49,13 +49,14 @@ def test_four1_spectrum_host(nr, form, log2n, kind):
     ref = x.copy()
     O.four1(ref, nn, 1)
     want = O.magnitude_spectrum(ref) if kind == "magnitude" else O.power_spectrum(ref)
-    d = x.copy()
-    nr.launch_count(reset=True)
-    got = nr.four1_spectrum(d, nn, 1, kind=kind, form=form)
-    n_spec = nr.launch_count(reset=True)
     e = x.copy()
+    nr.four1(e.copy(), nn, 1, form=form)  # first use of the form fills its twiddle table
+    nr.launch_count(reset=True)
     nr.four1(e, nn, 1, form=form)
     n_plain = nr.launch_count(reset=True)
+    d = x.copy()
+    got = nr.four1_spectrum(d, nn, 1, kind=kind, form=form)
+    n_spec = nr.launch_count(reset=True)
     assert n_spec <= max(n_plain, 1), (n_spec, n_plain)
     _close(form, d, ref, log2n, "four1_spectrum data")
     # |X|^2 doubles the relative error of X
