@@ -1089,6 +1089,65 @@ __device__ __forceinline__ typename F::C twist_elem(typename F::C own, typename 
   return F::add(h1, F::mul(h2, twiddle<F>(tw, logn, (unsigned)k, IS)));
 }
 
+// rlft3 form: h1 + w h2 for a twiddle w that is 1 at k = 0 (no DC packing;
+// the k3 = 0 plane pairs with speq).  mate, when given, receives the value of
+// the partner slot, conj(h1 - w h2).
+template <class F, int IS>
+__device__ __forceinline__ typename F::C twist_gen(typename F::C own, typename F::C part,
+                                                   long long k, int logn, const Twiddles& tw,
+                                                   typename F::C* mate = nullptr) {
+  using C = typename F::C;
+  const C cp = F::conj(part);
+  const C h1 = F::scale(F::add(own, cp), 0.5);
+  const C h2 = F::scale(F::mul_j(F::sub(own, cp), -IS), 0.5);
+  const C t = (k == 0) ? h2 : F::mul(h2, twiddle<F>(tw, logn, (unsigned)k, IS));
+  if (mate) *mate = F::conj(F::sub(h1, t));
+  return F::add(h1, t);
+}
+
+// rlft3 mirror-line tiling of a pass whose lines form a U x V grid (line
+// (u, v) = u V + v; U = 2^logU, V = 2^logV).  A line pairs with
+// ((U - u) mod U, (V - v) mod V).  Rows u = 0 and U/2 pair with themselves
+// and are tiled as a 1-D mirror tiling (mirror_col); the other rows go in
+// pairs (u, U - u): a tile takes C/2 consecutive lines of row u and their
+// C/2 mirrors in row U - u.  Tiles run [row 0][row U/2][row pairs].  Returns
+// the line of tile column c, its (u, v), and in c2 the tile column of its
+// mirror line.
+__device__ __forceinline__ long long mirror_line(long long tile, int c, int logC, int logU,
+                                                 int logV, int& c2, long long& v_out,
+                                                 long long& u_out) {
+  const long long U = 1ll << logU, V = 1ll << logV;
+  const int Cn = 1 << logC, half = Cn >> 1;
+  const long long tpr = V >> logC;  // tiles of a self-paired row
+  long long u0, u1, tl;
+  bool self;
+  if (tile < tpr) { u0 = u1 = 0; tl = tile; self = true; }
+  else if (U > 1 && tile < 2 * tpr) { u0 = u1 = U >> 1; tl = tile - tpr; self = true; }
+  else {
+    const long long t2 = tile - 2 * tpr;
+    const int logper = logV - logC + 1;  // 2V/C tiles per row pair
+    u0 = 1 + (t2 >> logper);
+    u1 = U - u0;
+    tl = t2 & ((1ll << logper) - 1);
+    self = false;
+  }
+  long long u, v;
+  if (c < half) {
+    u = u0;
+    v = tl * half + c;
+  } else {
+    u = u1;
+    v = V - (tl + 1) * half + 1 + (c - half);
+    if (v == V) v = self ? (V >> 1) : 0;
+  }
+  if (self && tl == 0 && c == 0) c2 = 0;
+  else if (self && tl == 0 && c == Cn - 1) c2 = Cn - 1;
+  else c2 = Cn - 1 - c;
+  u_out = u;
+  v_out = v;
+  return u * V + v;
+}
+
 template <class F>
 __device__ __forceinline__ typename F::C gload_rt(int io, const void* p, long long i) {
   if (io == IO_D2) return gload<F, IO_D2>(p, i);
@@ -1118,9 +1177,17 @@ __global__ void __launch_bounds__(T) k_twist_pass(PassParams p, int in_io, int o
   const int logn = p.logL + 1;  // n = 2L reals
   long long line0, j0;
   tile_origin(p, blockIdx.x, line0, j0);
-  const bool mir = p.mode == 0;  // multi-pass: mirror tiles; else whole lines
+  const bool r3 = p.twist == 2 || p.twist == -2;  // rlft3: mirror lines
+  const bool mir = !r3 && p.mode == 0;           // realft multi-pass: mirror columns
   const long long NC = p.L >> logR;
   const long long tl = mir ? (j0 >> logC) : 0;
+  // line of tile column c (whole-line tiles)
+  auto line_of = [&](int c) -> long long {
+    if (!r3) return line0 + c;
+    int c2;
+    long long u, v;
+    return mirror_line(blockIdx.x, c, logC, p.mirror_logU, p.mirror_logV, c2, v, u);
+  };
   // 1. load the tile (all loads first), inter-pass twiddles, stage
   {
     C v[kEPT];
@@ -1128,7 +1195,7 @@ __global__ void __launch_bounds__(T) k_twist_pass(PassParams p, int in_io, int o
     for (int k = 0; k < kEPT; ++k) {
       int c, r;
       elem_cr(tid + k * T, p.in_rcontig, logR, logC, c, r);
-      const long long line = mir ? line0 : line0 + c;
+      const long long line = mir ? line0 : line_of(c);
       const long long j = mir ? mirror_col(tl, c, logC, NC) : j0;
       v[k] = (line < p.nlines)
                  ? gload_rt<F>(in_io, p.in, line_base(p, line) + (j + (long long)r * NC) * p.s)
@@ -1156,6 +1223,23 @@ __global__ void __launch_bounds__(T) k_twist_pass(PassParams p, int in_io, int o
       const int e = tid + k * T;
       const int c = e & (Cn - 1), r = e >> logC;
       int c2 = c, r2 = (R - r) & (R - 1);
+      if (r3) {
+        // rows are i3 (R = nn3/2 points); row 0 pairs with speq at the
+        // mirrored (i1, i2), the others with row R - r of the mirror line
+        long long u, vv;
+        mirror_line(blockIdx.x, c, logC, p.mirror_logU, p.mirror_logV, c2, vv, u);
+        C part;
+        if (r == 0) {
+          const long long U = 1ll << p.mirror_logU, V = 1ll << p.mirror_logV;
+          const d2 sq =
+              reinterpret_cast<const d2*>(p.aux)[((U - u) & (U - 1)) * V + ((V - vv) & (V - 1))];
+          part = F::from_d(sq.x, sq.y);
+        } else {
+          part = F::from_s(sm[c2 * cs + pidx(r2, sh)]);
+        }
+        tv[k] = twist_gen<F, -1>(F::from_s(sm[c * cs + pidx(r, sh)]), part, r, logR + 1, p.tw);
+        continue;
+      }
       if (mir) mirror_partner(tl, c, r, logC, logR, c2, r2);
       const long long kk = mir ? mirror_col(tl, c, logC, NC) + (long long)r * NC : r;
       tv[k] = twist_elem<F, -1>(F::from_s(sm[c * cs + pidx(r, sh)]),
@@ -1176,16 +1260,36 @@ __global__ void __launch_bounds__(T) k_twist_pass(PassParams p, int in_io, int o
   for (int k = 0; k < kEPT; ++k) {
     int c, r;
     elem_cr(tid + k * T, p.out_rcontig, logR, logC, c, r);
-    const long long line = mir ? line0 : line0 + c;
+    int c3 = c;
+    long long u3 = 0, v3 = 0;
+    const long long line =
+        mir ? line0
+            : (r3 ? mirror_line(blockIdx.x, c, logC, p.mirror_logU, p.mirror_logV, c3, v3, u3)
+                  : line0 + c);
     if (line >= p.nlines) continue;
     const long long j = mir ? mirror_col(tl, c, logC, NC) : j0;
     const long long jd = ((j >> p.logNs) << (p.logNs + logR)) + (j & (p.Ns - 1));
     C v = F::from_s(sm[c * cs + pidx(r, sh)]);
     if constexpr (SG > 0) {
       int c2 = c, r2 = (R - r) & (R - 1);
-      if (mir) mirror_partner(tl, c, r, logC, logR, c2, r2);
-      v = twist_elem<F, 1>(v, F::from_s(sm[c2 * cs + pidx(r2, sh)]), jd + (long long)r * p.Ns,
-                           logn, p.tw);
+      if (r3) {
+        // rows are i1 (the axis-0 pass); the twist runs along i3 = v3 of the
+        // line; the i3 = 0 lines also write speq at the mirrored (i1, i2)
+        C mate;
+        v = twist_gen<F, 1>(v, F::from_s(sm[c3 * cs + pidx(r2, sh)]), v3, p.mirror_logV + 1,
+                            p.tw, &mate);
+        if (v3 == 0) {
+          const long long U = 1ll << p.mirror_logU;
+          double mx, my;
+          F::to_d(mate, mx, my);
+          reinterpret_cast<d2*>(p.aux)[(long long)((R - r) & (R - 1)) * U + ((U - u3) & (U - 1))] =
+              d2{mx, my};
+        }
+      } else {
+        if (mir) mirror_partner(tl, c, r, logC, logR, c2, r2);
+        v = twist_elem<F, 1>(v, F::from_s(sm[c2 * cs + pidx(r2, sh)]), jd + (long long)r * p.Ns,
+                             logn, p.tw);
+      }
     }
     if (p.do_scale) v = apply_scale<F>(v, p);
     gstore_rt<F>(out_io, p.out, line_base(p, line) + (jd + (long long)r * p.Ns) * p.s, v);

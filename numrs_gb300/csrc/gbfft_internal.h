@@ -86,11 +86,19 @@ struct PassParams {
   // (spec_kind 2); 0 = off.
   double* spec;
   int spec_kind;
-  // realft twist fused into this pass (src/Real_FT.rs:24-46,120-142):
-  // +1 = forward twist after the last pass of the forward FFT, -1 = inverse
-  // twist before the first pass of the inverse FFT; 0 = none.  Lines have
-  // L = n/2 points; the pass runs as k_twist_pass.
+  // Real-transform twist fused into this pass (the pass runs as k_twist_pass):
+  //   +1 / -1  realft (src/Real_FT.rs:24-46,120-142): forward twist after the
+  //            last pass of the forward FFT / inverse twist before the first
+  //            pass of the inverse FFT; lines have L = n/2 points
+  //   +2 / -2  rlft3 (src/Real_FT3.rs:58-127): the forward twist in the last
+  //            (axis-0) pass of the forward 3-D FFT, the inverse twist in the
+  //            first (last-axis) pass of the inverse; the pass's lines form a
+  //            grid of 2^mirror_logU x 2^mirror_logV lines, and aux is speq
+  //   0        none
   int twist;
+  int mirror_logU;
+  int mirror_logV;
+  double* aux;
   // Per-slot parts of the global element indices of a tile, for layouts
   // without per-line pointer tables: slot k of thread tid holds tile element
   // e = tid + k*T, and its index is a per-thread base plus in_off[k] (load

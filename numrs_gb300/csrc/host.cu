@@ -371,12 +371,30 @@ int launch_pass(Form f, int sign, IOType in, IOType out, const PassParams& p, in
 
 // Run an axis plan on `data` (interleaved double complex, device memory).
 // spec/spec_kind: optional spectrum epilogue of the last pass (see PassParams).
+// Work riding on an axis plan's first or last pass.
+struct AxisExtras {
+  double* spec = nullptr;  // spectrum epilogue of the last pass (PassParams)
+  int spec_kind = 0;
+  int twist = 0;           // real-transform twist (PassParams::twist): > 0 on
+                           // the last pass, < 0 on the first
+  int logU = 0, logV = 0;  // rlft3: the pass's line grid
+  double* aux = nullptr;   // rlft3: speq
+};
+
 // twist: realft twist fused into the last (+1) or first (-1) pass.
 // ext_scratch: scratch supplied by the caller (at least 16 bytes per complex
 // element of the axis' span) instead of the library's device scratch.
+// ex: the extras as one record (replaces spec, spec_kind and twist).
 int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale = 1.0,
              double* spec = nullptr, int spec_kind = 0, int twist = 0,
-             void* ext_scratch = nullptr) {
+             void* ext_scratch = nullptr, const AxisExtras* ex = nullptr) {
+  AxisExtras local;
+  if (!ex) {
+    local.spec = spec;
+    local.spec_kind = spec_kind;
+    local.twist = twist;
+    ex = &local;
+  }
   Twiddles tw;
   TRY(tables(f, tw));
   const IOType sio = scratch_io(f);
@@ -413,11 +431,16 @@ int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale = 1.
       p.do_scale = 1;
       p.scale = scale;
     }
-    if (last && spec_kind) {
-      p.spec = spec;
-      p.spec_kind = spec_kind;
+    if (last && ex->spec_kind) {
+      p.spec = ex->spec;
+      p.spec_kind = ex->spec_kind;
     }
-    if ((twist > 0 && last) || (twist < 0 && first)) p.twist = twist;
+    if ((ex->twist > 0 && last) || (ex->twist < 0 && first)) {
+      p.twist = ex->twist;
+      p.mirror_logU = ex->logU;
+      p.mirror_logV = ex->logV;
+      p.aux = ex->aux;
+    }
     TRY(launch_pass(f, sign, in_t, out_t, p, ps.threads));
   }
   return GBFFT_OK;
@@ -697,22 +720,45 @@ int realft_dev(Form f, double* d, long long n, int isign, long long batch = 1,
   return GBFFT_OK;
 }
 
-// fourn on device data
-int fourn_dev(Form f, double* d, const long long* nn, int ndim, int isign) {
-  long long total = 1;
+// The plan of axis dd of an N-D array of dims nn (row-major, last axis
+// contiguous).
+const AxisPlan& nd_axis_plan(Form f, const long long* nn, int ndim, int dd) {
+  long long total = 1, s = 1;
   for (int i = 0; i < ndim; ++i) total *= nn[i];
-  long long s = 1;
+  for (int i = ndim - 1; i > dd; --i) s *= nn[i];
+  const long long L = nn[dd], nl = total / L;
+  if (s == 1) return axis_plan(L, 1, nl, 0, L, f);
+  return axis_plan(L, s, nl, ilog2((unsigned long long)s), L * s, f);
+}
+
+// The plan for the rlft3 twist riding on a single-pass plan whose lines form
+// a 2^logU x 2^logV grid: tiles of whole lines, C >= 2 columns and at most
+// one grid row of them (the mirror-line tiling), at least one warp per tile.
+// Returns false when the plan does not qualify.
+bool rlft3_twist_plan(const AxisPlan& base, int logU, int logV, AxisPlan& out) {
+  if (base.passes.size() != 1) return false;
+  const PassParams& b = base.passes[0].p;
+  if (b.mode != 1 || logU < 1 || b.nlines != (1ll << (logU + logV))) return false;
+  const int logC = std::min(b.logC, logV);
+  if (logC < 1 || b.logR + logC < 9) return false;
+  out = base;
+  Pass& ps = out.passes[0];
+  ps.p.logC = logC;
+  ps.threads = (1 << (b.logR + logC)) / 16;
+  ps.p.tiles = (b.L >> b.logR) * (b.nlines >> logC);
+  return true;
+}
+
+// fourn on device data.  ex (3-D only): the rlft3 twist on the last axis
+// processed (axis 0, forward) or the first (the last axis, inverse), whose
+// plan is twist_plan.
+int fourn_dev(Form f, double* d, const long long* nn, int ndim, int isign,
+              const AxisExtras* ex = nullptr, const AxisPlan* twist_plan = nullptr) {
   for (int dd = ndim - 1; dd >= 0; --dd) {
-    long long L = nn[dd];
-    if (L > 1) {
-      long long nl = total / L;
-      if (s == 1) {
-        TRY(run_axis(f, isign, axis_plan(L, 1, nl, 0, L, f), d));
-      } else {
-        TRY(run_axis(f, isign, axis_plan(L, s, nl, ilog2((unsigned long long)s), L * s, f), d));
-      }
-    }
-    s *= L;
+    if (nn[dd] <= 1) continue;
+    const bool with = ex && ((ex->twist > 0 && dd == 0) || (ex->twist < 0 && dd == ndim - 1));
+    TRY(run_axis(f, isign, with ? *twist_plan : nd_axis_plan(f, nn, ndim, dd), d, 1.0, nullptr, 0,
+                 0, nullptr, with ? ex : nullptr));
   }
   return GBFFT_OK;
 }
@@ -1432,16 +1478,44 @@ int gbfft_rlft3(double* data, double* speq, size_t nn1, size_t nn2, size_t nn3, 
   TRY(stage_inout(c, g.stage_a, data, total, &d));
   TRY(stage_inout(c, g.stage_b, speq, 2 * nn1 * nn2, &sp, isign == -1));
   long long dims[3] = {(long long)nn1, (long long)nn2, (long long)(nn3 / 2)};
+  // The twist rides on the forward FFT's last pass (axis 0, whose lines form
+  // the nn2 x nn3/2 grid) or the inverse FFT's first pass (the last axis,
+  // lines on the nn1 x nn2 grid) when those are single passes; otherwise it
+  // runs as its own kernels.
+  AxisExtras ex;
+  ex.twist = 2 * isign;
+  ex.aux = sp;
+  bool fused = nn1 >= 2 && nn2 >= 2 && nn3 >= 4;
+  AxisPlan tplan;
+  if (fused) {
+    if (isign == 1) {
+      ex.logU = ilog2(nn2);
+      ex.logV = ilog2(nn3 / 2);
+      fused = rlft3_twist_plan(nd_axis_plan(c.form(), dims, 3, 0), ex.logU, ex.logV, tplan);
+    } else {
+      ex.logU = ilog2(nn1);
+      ex.logV = ilog2(nn2);
+      fused = rlft3_twist_plan(nd_axis_plan(c.form(), dims, 3, 2), ex.logU, ex.logV, tplan);
+    }
+  }
   if (isign == 1) {
-    TRY(fourn_dev(c.form(), d, dims, 3, 1));
-    CK(launch_rlft3_speq(d, sp, nn1, nn2, nn3, g.cur));
-    g.launches++;
-    CK(launch_rlft3_twist(c.form(), 1, d, sp, nn1, nn2, nn3, tw, g.cur));
-    g.launches++;
+    if (fused) {
+      TRY(fourn_dev(c.form(), d, dims, 3, 1, &ex, &tplan));
+    } else {
+      TRY(fourn_dev(c.form(), d, dims, 3, 1));
+      CK(launch_rlft3_speq(d, sp, nn1, nn2, nn3, g.cur));
+      g.launches++;
+      CK(launch_rlft3_twist(c.form(), 1, d, sp, nn1, nn2, nn3, tw, g.cur));
+      g.launches++;
+    }
   } else {
-    CK(launch_rlft3_twist(c.form(), -1, d, sp, nn1, nn2, nn3, tw, g.cur));
-    g.launches++;
-    TRY(fourn_dev(c.form(), d, dims, 3, -1));
+    if (fused) {
+      TRY(fourn_dev(c.form(), d, dims, 3, -1, &ex, &tplan));
+    } else {
+      CK(launch_rlft3_twist(c.form(), -1, d, sp, nn1, nn2, nn3, tw, g.cur));
+      g.launches++;
+      TRY(fourn_dev(c.form(), d, dims, 3, -1));
+    }
   }
   TRY(unstage(c, data, d, total));
   TRY(unstage(c, speq, sp, 2 * nn1 * nn2));
@@ -1820,8 +1894,6 @@ int gbfft_correl_normalized(const double* data1, size_t n1, const double* data2,
   const double s2 = fast ? std::sqrt(h[3] / nd - m2 * m2) : std::sqrt(h[3] / nd);
   if (s1 == 0.0 || s2 == 0.0 || std::isnan(s1) || std::isnan(s2))
     return fail(GBFFT_ZERO_STD_DEV, "Normalization error: standard deviation is zero");
-  double* out = ans;
-  if (!c.dev()) out = za;  // result staged in the z buffer after use below
   if (fast && n <= 32) {
     double* o = c.dev() ? ans : zb;
     CK(launch_correl_direct_centered(a, b, o, (long long)n, m1, m2, 1.0 / (s1 * s2 * nd), g.cur));
@@ -1844,7 +1916,6 @@ int gbfft_correl_normalized(const double* data1, size_t n1, const double* data2,
   TRY(d2d(w, za, n * sizeof(double)));
   TRY(d2d(w + n, zb, n * sizeof(double)));
   TRY(spectral_dev(c.form(), 2, w, (long long)n));
-  (void)out;
   if (c.dev()) TRY(d2d(ans, w, n * sizeof(double)));
   else TRY(d2h(ans, w, n * sizeof(double)));
   return ss.finish(c);

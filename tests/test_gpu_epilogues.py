@@ -151,3 +151,61 @@ def test_twofft_path_device_tensors(nr, twofft_path):
     st, want = O.convlv(x, taps, 1)
     got = nr.convlv(torch.from_numpy(x).cuda(), torch.from_numpy(taps).cuda(), 1)
     assert rel_l2(got.cpu().numpy(), want) <= 1e-12
+
+
+# ---------------------------------------------------------------------------
+# realft and rlft3 with the twist fused into a pass: results as the oracle's,
+# and no separate twist kernel in the launch list
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("log2n", [2, 3, 5, 9, 11, 13, 14, 18, 21, 23])
+@pytest.mark.parametrize("isign", [1, -1])
+def test_realft_fused_twist(nr, form, log2n, isign):
+    import oracle as O
+    from numrs_gb300 import workloads as W
+    n = 1 << log2n
+    x = W.normal(6000 + log2n, n)
+    if isign == -1:
+        O.realft(x, n, 1)  # a packed spectrum as input
+    ref = x.copy()
+    O.realft(ref, n, isign)
+    d = x.copy()
+    nr.realft(d.copy(), n, isign, form=form)  # tables of the form
+    nr.launch_count(reset=True)
+    nr.realft(d, n, isign, form=form)
+    launches = nr.launch_count(reset=True)
+    _close(form, d, ref, log2n, "realft %d isign %d" % (n, isign))
+    # the transform's passes only: 2^(log2n-1) complex points in at most 3 passes
+    assert launches <= 3, launches
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("shape", [(2, 2, 4), (4, 8, 16), (16, 8, 4), (8, 4, 64), (32, 64, 128),
+                                   (64, 2, 32), (2, 128, 8)])
+def test_rlft3_fused_twist(nr, form, shape):
+    import oracle as O
+    from numrs_gb300 import workloads as W
+    n1, n2, n3 = shape
+    x = W.plane_waves(shape, count=4).ravel()
+    ref, rs = x.copy(), np.zeros(n1 * 2 * n2)
+    O.rlft3(ref, rs, n1, n2, n3, 1)
+    log2n = int(np.log2(n1 * n2 * n3))
+    d = x.copy()
+    sp = np.zeros(n1 * 2 * n2)
+    nr.rlft3(d.copy(), sp.copy(), n1, n2, n3, 1, form=form)
+    nr.launch_count(reset=True)
+    nr.rlft3(d, sp, n1, n2, n3, 1, form=form)
+    fwd_launches = nr.launch_count(reset=True)
+    _close(form, np.concatenate([d, sp]), np.concatenate([ref, rs]), log2n, "rlft3 fwd %s" % (shape,))
+    # shapes whose twist passes qualify: one pass per axis, no speq gather or
+    # twist kernel
+    if shape in ((32, 64, 128), (64, 2, 32)):
+        assert fwd_launches <= 3, fwd_launches
+    d2, s2 = ref.copy(), rs.copy()
+    nr.launch_count(reset=True)
+    nr.rlft3(d2, s2, n1, n2, n3, -1, form=form)
+    inv_launches = nr.launch_count(reset=True)
+    O.rlft3(ref, rs, n1, n2, n3, -1)
+    _close(form, d2, ref, log2n, "rlft3 inverse %s" % (shape,))
+    if shape in ((32, 64, 128), (2, 128, 8)):
+        assert inv_launches <= 3, inv_launches

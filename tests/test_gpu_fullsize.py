@@ -197,8 +197,11 @@ def test_rlft3_512cubed(env, rlft3_case, form):
     n = int(np.prod(nn))
     d = torch.from_numpy(x).cuda()
     sp = torch.zeros(nn[0] * 2 * nn[1], dtype=torch.float64, device="cuda")
+    nr.launch_count(reset=True)
     nr.rlft3(d, sp, nn[0], nn[1], nn[2], 1, form=form)
     torch.cuda.synchronize()
+    # one pass per axis; the twist and the speq plane ride on the last one
+    assert nr.launch_count(reset=True) <= 4
     got = np.concatenate([d.cpu().numpy(), sp.cpu().numpy()])
     _check(form, got, np.concatenate([ref, speq]), int(math.log2(n)), "rlft3 512^3 %s" % form)
     nr.rlft3(d, sp, nn[0], nn[1], nn[2], -1, form=form)
