@@ -75,8 +75,12 @@ size_t gbfft_scratch_bytes(void);
 int gbfft_release(void);
 /* Autotuner (no counterpart in the crate): when enabled, the first plan of
  * each axis shape and form times candidate tile sizes on a scratch array and
- * keeps the fastest (also GBFFT_AUTOTUNE=1; GBFFT_TUNE_CACHE=<file> keeps the
- * choices across processes).  Tuning synchronises the device once per shape. */
+ * keeps the fastest, and the first batch of each signature (form, direction,
+ * multiset of sizes) times candidate schedules of the persistent launch --
+ * the first-pass radix of every bin above 4096 points and the resident CTAs
+ * per SM -- on a zeroed device copy of the batch (also GBFFT_AUTOTUNE=1;
+ * GBFFT_TUNE_CACHE=<file> keeps the choices across processes).  Tuning
+ * synchronises the device once per shape or signature. */
 int gbfft_set_autotune(int enable);
 /* Forward transforms of gbfft_convlv / gbfft_correl (no counterpart switch in
  * the crate; the batched forms always use path 0, which transforms a shared
@@ -105,12 +109,17 @@ long long gbfft_launch_count(int reset);
  *                                 for, so that its wait cannot be met and
  *                                 must run out (the call returns
  *                                 GBFFT_TIMEOUT); 0 = off
+ *   GBFFT_DEBUG_BATCH_FIRST_RADIX_DELTA  shifts the first-pass radix of the
+ *                                 batch launch's two-pass bins away from
+ *                                 half the length (the splits the autotuner
+ *                                 tries), so tests can check each one
  * The batch settings drop the cached batch plan.  Nothing here hangs or
  * faults a GPU: every device wait stays bounded. */
 enum {
   GBFFT_DEBUG_FAIL_ALLOC_AT = 1,
   GBFFT_DEBUG_BATCH_SPIN_LIMIT = 2,
-  GBFFT_DEBUG_BATCH_NEED_EXTRA = 3
+  GBFFT_DEBUG_BATCH_NEED_EXTRA = 3,
+  GBFFT_DEBUG_BATCH_FIRST_RADIX_DELTA = 4
 };
 int gbfft_debug_set(int key, long long value);
 int gbfft_profile(int enable);  /* also clears the records */

@@ -69,6 +69,7 @@ SIGNATURES = {
 DEBUG_FAIL_ALLOC_AT = 1
 DEBUG_BATCH_SPIN_LIMIT = 2
 DEBUG_BATCH_NEED_EXTRA = 3
+DEBUG_BATCH_FIRST_RADIX_DELTA = 4
 
 _lib = None
 

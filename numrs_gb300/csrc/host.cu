@@ -21,7 +21,6 @@ namespace gbfft {
 
 namespace {
 
-constexpr int kTileE = 4096;     // complex elements per CTA tile
 constexpr int kMaxPassLog = 10;  // radix of a pass in a multi-pass schedule
 constexpr int kMaxAxisLog = kMaxLog;
 
@@ -73,6 +72,7 @@ struct Ctx {
   long long alloc_calls = 0;
   unsigned int dbg_spin_limit = 0;
   unsigned int dbg_need_extra = 0;
+  int dbg_first_radix_delta = 0;  // shifts the default two-pass batch split
   // convlv/correl forward transforms: 0 = the two inputs as two n/2-point
   // realft lines, 1 = packed as one n-point complex FFT (twofft)
   int spectral_path = 0;
@@ -273,15 +273,20 @@ constexpr int kLatencyTileLog = 9;
 
 // tileLog: log2 of the complex elements per CTA tile (10..12); multi-pass
 // radices are kept 4 columns below it so that strided rows stay >= 64 bytes.
+// radices: an explicit pass schedule (log2 radix of each pass, summing to
+// log2 L, each at most tileLog) instead of the default one.
 AxisPlan make_axis_plan(long long L, long long s, long long nlines, int lq_log,
-                        long long lstride, bool full_tile = false, int tileLog = 12) {
+                        long long lstride, bool full_tile = false, int tileLog = 12,
+                        const std::vector<int>* radices = nullptr) {
   AxisPlan ap;
   const int logL = ilog2((unsigned long long)L);
   const int maxPassLog = std::min(kMaxPassLog, tileLog - 2);
   std::vector<int> radix;
   const bool latency = !full_tile && s == 1 && logL >= 10 && logL <= 12 &&
                        L * nlines <= kLatencyMaxWork;
-  if (latency) {
+  if (radices) {
+    radix = *radices;
+  } else if (latency) {
     radix.push_back((logL + 1) / 2);
     radix.push_back(logL / 2);
   } else if (logL <= tileLog) {
@@ -508,8 +513,12 @@ void tune_load() {
   if (!fp) return;
   long long L, s, nl, ls;
   int lq, f, tl;
-  while (fscanf(fp, "%lld %lld %lld %d %lld %d %d", &L, &s, &nl, &lq, &ls, &f, &tl) == 7)
-    g_tuned[std::make_tuple(L, s, nl, lq, ls, f)] = tl;
+  char line[8192];
+  while (fgets(line, sizeof line, fp)) {
+    // tile lines; the batch tuner's lines start with "batch"
+    if (sscanf(line, "%lld %lld %lld %d %lld %d %d", &L, &s, &nl, &lq, &ls, &f, &tl) == 7)
+      g_tuned[std::make_tuple(L, s, nl, lq, ls, f)] = tl;
+  }
   fclose(fp);
 }
 
@@ -813,8 +822,30 @@ void batch_plan_free(BatchPlan& b) {
   b.valid = false;
 }
 
+// Pass schedule of the persistent batch launch, chosen by the autotuner: per
+// bin length above 4096 points, the log2 radix of the first of its two passes
+// (absent: half the length, rounded up), and the resident CTAs per SM (0: the
+// occupancy maximum).
+struct BatchTune {
+  std::map<long long, int> first_radix;
+  int per = 0;
+};
+
+// The passes of a bin of length L under a tune record (nullptr: default).
+std::vector<int> batch_radices(long long L, const BatchTune* tune) {
+  const int logL = ilog2((unsigned long long)L);
+  int first = -1;
+  if (tune) {
+    auto it = tune->first_radix.find(L);
+    if (it != tune->first_radix.end()) first = it->second;
+  }
+  if (logL <= 12) return {logL};
+  if (first < 0) first = std::min(12, std::max(logL - 12, (logL + 1) / 2 + g.dbg_first_radix_delta));
+  return {first, logL - first};
+}
+
 int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const size_t* nn,
-                     size_t count, bool host_ptrs) {
+                     size_t count, bool host_ptrs, const BatchTune* tune = nullptr) {
   batch_plan_free(b);
   b.nn.assign(nn, nn + count);
   b.ptrs.assign((const void* const*)dptrs, (const void* const*)dptrs + count);
@@ -841,7 +872,7 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
   const IOType sio = scratch_io(f);
   size_t scratch_elems = 0;
   for (auto& bn : bins)
-    if (bn.L > kTileE) scratch_elems += (size_t)(bn.L * bn.count);
+    if (bn.L > 1 && batch_radices(bn.L, tune).size() == 2) scratch_elems += (size_t)(bn.L * bn.count);
   if (scratch_elems) TRY(ensure(b.scratch, scratch_elems * io_bytes(sio)));
   Twiddles tw;
   TRY(tables(f, tw));
@@ -849,7 +880,8 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
   size_t soff = 0;
   for (auto& bn : bins) {
     if (bn.L == 1) continue;  // 1-point transforms are the identity
-    AxisPlan ap = make_axis_plan(bn.L, 1, bn.count, 0, bn.L, true);
+    const std::vector<int> rad = batch_radices(bn.L, tune);
+    AxisPlan ap = make_axis_plan(bn.L, 1, bn.count, 0, bn.L, true, 12, &rad);
     if (ap.passes.size() == 1) {
       BatchRange r;
       std::memset(&r, 0, sizeof r);
@@ -921,6 +953,7 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
   // (bulk copies are not used on host memory)
   b.prefetch = f != FORM_F64 && aligned && !host_ptrs && pfenv && pfenv[0] == '1';
   int per = b.prefetch ? batch_pf_blocks_per_sm(f, sign) : batch_blocks_per_sm(f, sign);
+  if (tune && tune->per > 0 && tune->per < per) per = tune->per;
   if (per < 1) per = 1;
   b.grid = (int)std::min<long long>((long long)dev_sms * per, std::max<long long>(item, 1));
   // capture [reset counters, persistent launch] on the library stream
@@ -955,6 +988,177 @@ bool batch_plan_matches(const BatchPlan& b, Form f, int sign, double* const* dpt
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner of the persistent batch launch (on when autotuning is: the
+// GBFFT_AUTOTUNE=1 switch or gbfft_set_autotune).  For a batch signature (form,
+// direction, the multiset of sizes) it times candidate schedules -- per size
+// bin one pass or two passes with the first radix around half the length,
+// and the resident CTAs per SM -- on a zeroed device copy of the batch (the
+// caller's arrays are never touched), by coordinate descent from the default
+// schedule: bins in decreasing order of work, then the grid.  Each candidate is
+// one CUDA-graph replay timed with events (best of three after one warm-up).
+// Results live for the process and, with GBFFT_TUNE_CACHE, in that file.
+// ---------------------------------------------------------------------------
+std::map<std::string, BatchTune> g_batch_tuned;
+bool g_batch_tune_loaded = false;
+
+std::string batch_signature(Form f, int sign, const size_t* nn, size_t count) {
+  std::map<size_t, size_t> bins;
+  for (size_t i = 0; i < count; ++i) bins[nn[i]]++;
+  std::string k = std::to_string((int)f) + "," + std::to_string(sign);
+  for (auto& b : bins) k += ";" + std::to_string(b.first) + "x" + std::to_string(b.second);
+  return k;
+}
+
+std::string tune_str(const BatchTune& t) {
+  std::string s = std::to_string(t.per);
+  for (auto& fr : t.first_radix) s += " " + std::to_string(fr.first) + ":" + std::to_string(fr.second);
+  return s;
+}
+
+void batch_tune_load() {
+  if (g_batch_tune_loaded) return;
+  g_batch_tune_loaded = true;
+  if (g.tune_cache.empty()) return;
+  FILE* fp = fopen(g.tune_cache.c_str(), "r");
+  if (!fp) return;
+  char line[8192];
+  while (fgets(line, sizeof line, fp)) {
+    // "batch <signature> <per> <L>:<first> ..."
+    if (strncmp(line, "batch ", 6) != 0) continue;
+    char sig[4096];
+    int per = 0, n = 0;
+    if (sscanf(line + 6, "%4095s %d%n", sig, &per, &n) != 2) continue;
+    BatchTune t;
+    t.per = per;
+    const char* q = line + 6 + n;
+    long long L;
+    int fr, m;
+    while (sscanf(q, " %lld:%d%n", &L, &fr, &m) == 2) {
+      t.first_radix[L] = fr;
+      q += m;
+    }
+    g_batch_tuned[sig] = t;
+  }
+  fclose(fp);
+}
+
+// Time one candidate schedule on the scratch arrays: best of three replays.
+float time_batch(Form f, int sign, double* const* tp, const size_t* nn, size_t count,
+                 const BatchTune& t, cudaEvent_t a, cudaEvent_t b) {
+  BatchPlan bp;
+  float best = 1e30f;
+  if (build_batch_plan(bp, f, sign, tp, nn, count, false, &t) == GBFFT_OK) {
+    cudaGraphLaunch(bp.exec, g.cur);
+    for (int r = 0; r < 3; ++r) {
+      cudaEventRecord(a, g.cur);
+      cudaGraphLaunch(bp.exec, g.cur);
+      cudaEventRecord(b, g.cur);
+      cudaEventSynchronize(b);
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess && ms < best) best = ms;
+    }
+  }
+  batch_plan_free(bp);
+  cudaGetLastError();
+  return best;
+}
+
+BatchTune tune_batch(Form f, int sign, const size_t* nn, size_t count) {
+  BatchTune best;
+  size_t total = 0;
+  for (size_t i = 0; i < count; ++i) total += 2 * nn[i];
+  void* buf = nullptr;
+  if (total * sizeof(double) > (size_t(8) << 30) || dev_alloc(&buf, total * sizeof(double)) != cudaSuccess)
+    return best;  // too large to copy for tuning: keep the default schedule
+  cudaMemsetAsync(buf, 0, total * sizeof(double), g.cur);
+  std::vector<double*> tp(count);
+  size_t off = 0;
+  for (size_t i = 0; i < count; ++i) {
+    tp[i] = (double*)buf + off;
+    off += 2 * nn[i];
+  }
+  const bool prof = g.profiling;
+  g.profiling = false;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  // bins in decreasing order of work
+  std::map<size_t, size_t> bins;
+  for (size_t i = 0; i < count; ++i) bins[nn[i]]++;
+  std::vector<std::pair<double, long long>> order;
+  for (auto& bn : bins)
+    if (bn.first > 1)
+      order.push_back({-(double)bn.first * bn.second * ilog2(bn.first), (long long)bn.first});
+  std::sort(order.begin(), order.end());
+  float cur = time_batch(f, sign, tp.data(), nn, count, best, a, b);
+  for (auto& o : order) {
+    const long long L = o.second;
+    const int logL = ilog2((unsigned long long)L);
+    const int def = (logL + 1) / 2;
+    // the persistent kernel's tiles are 4096 elements of one transform, so
+    // bins of up to 4096 points take one pass; longer ones choose the split
+    std::vector<int> cands;
+    if (logL > 12)
+      for (int r = (logL + 1) / 2 - 2; r <= (logL + 1) / 2 + 2; ++r)
+        if (r >= logL - 12 && r <= 12) cands.push_back(r);
+    if (cands.empty()) continue;
+    int keep = def;
+    for (int r : cands) {
+      if (r == def) continue;
+      BatchTune t = best;
+      t.first_radix[L] = r;
+      const float ms = time_batch(f, sign, tp.data(), nn, count, t, a, b);
+      if (g.tune_verbose)
+        fprintf(stderr, "gbfft batch tune L=%lld first=%d: %.4f ms (best %.4f)\n", L, r, ms, cur);
+      if (ms < cur * 0.98f) {
+        cur = ms;
+        keep = r;
+      }
+    }
+    best.first_radix[L] = keep;
+  }
+  const int occ = batch_blocks_per_sm(f, sign);
+  for (int per = occ - 1; per >= 1 && per >= occ - 2; --per) {
+    BatchTune t = best;
+    t.per = per;
+    const float ms = time_batch(f, sign, tp.data(), nn, count, t, a, b);
+    if (g.tune_verbose)
+      fprintf(stderr, "gbfft batch tune per=%d: %.4f ms (best %.4f)\n", per, ms, cur);
+    if (ms < cur * 0.98f) {
+      cur = ms;
+      best.per = per;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  g.profiling = prof;
+  cudaStreamSynchronize(g.cur);
+  cudaFree(buf);
+  cudaGetLastError();
+  return best;
+}
+
+// The tune record of a batch signature when autotuning is on (tuning it on
+// first sight), else nullptr.
+const BatchTune* batch_tune_for(Form f, int sign, const size_t* nn, size_t count) {
+  if (!g.autotune) return nullptr;
+  batch_tune_load();
+  const std::string sig = batch_signature(f, sign, nn, count);
+  auto it = g_batch_tuned.find(sig);
+  if (it != g_batch_tuned.end()) return &it->second;
+  BatchTune t = tune_batch(f, sign, nn, count);
+  auto ins = g_batch_tuned.emplace(sig, t).first;
+  if (!g.tune_cache.empty()) {
+    FILE* fp = fopen(g.tune_cache.c_str(), "a");
+    if (fp) {
+      fprintf(fp, "batch %s %s\n", sig.c_str(), tune_str(t).c_str());
+      fclose(fp);
+    }
+  }
+  return &ins->second;
+}
+
 // Transforms of at most 2^20 points go through the persistent launch; larger
 // ones (rare in a batch) run their own pass schedule.
 int run_batch_dev(Form f, int sign, double* const* dptrs, const size_t* nn, size_t count,
@@ -967,9 +1171,11 @@ int run_batch_dev(Form f, int sign, double* const* dptrs, const size_t* nn, size
   }
   if (!small_p.empty()) {
     if (!batch_plan_matches(g_batch, f, sign, small_p.data(), small_n.data(), small_p.size(),
-                            host_ptrs))
+                            host_ptrs)) {
+      const BatchTune* tune = batch_tune_for(f, sign, small_n.data(), small_n.size());
       TRY(build_batch_plan(g_batch, f, sign, small_p.data(), small_n.data(), small_p.size(),
-                           host_ptrs));
+                           host_ptrs, tune));
+    }
     {
       ProfScope ps(PK_PASS, 0.0);
       CK(cudaGraphLaunch(g_batch.exec, g.cur));
@@ -1135,6 +1341,11 @@ int gbfft_debug_set(int key, long long value) {
       if (value < 0) return fail(GBFFT_INVALID_ARG, "debug_set: negative allocation index");
       g.fail_alloc_at = value;
       g.alloc_calls = 0;
+      return GBFFT_OK;
+    case GBFFT_DEBUG_BATCH_FIRST_RADIX_DELTA:
+      if (value < -12 || value > 12) return fail(GBFFT_INVALID_ARG, "debug_set: value out of range");
+      g.dbg_first_radix_delta = (int)value;
+      batch_plan_free(g_batch);
       return GBFFT_OK;
     case GBFFT_DEBUG_BATCH_SPIN_LIMIT:
     case GBFFT_DEBUG_BATCH_NEED_EXTRA:
