@@ -45,6 +45,11 @@ int batch_blocks_per_sm(Form f, int sign);
 cudaError_t launch_batch_pf(Form f, int sign, const BatchParams& P, int grid, cudaStream_t st);
 int batch_pf_blocks_per_sm(Form f, int sign);
 
+// The tensor-core form on tcgen05 (batch_umma.cu): radix-16 sub-passes as
+// tcgen05.mma products with TMEM accumulators.
+cudaError_t launch_batch_umma(int sign, const BatchParams& P, int grid, cudaStream_t st);
+int batch_blocks_per_sm_umma(int sign);
+
 // per-form launchers (batch_<form>.cu), behind the dispatchers above
 cudaError_t launch_batch_f64(int sign, const BatchParams& P, int grid, cudaStream_t st);
 cudaError_t launch_batch_f32(int sign, const BatchParams& P, int grid, cudaStream_t st);

@@ -21,6 +21,7 @@
 #include "fft_core.cuh"
 #include "batch.h"
 #include "tma.cuh"
+#include "umma16.cuh"
 
 namespace gbfft {
 
@@ -74,6 +75,171 @@ __global__ void __launch_bounds__(256, (F::kind == 1 && !F::kTensor ? 3 : 2))
     }
     __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core form on tcgen05 (umma16.cuh): the same queue, pass-1 counters and
+// bounded waits as k_batch; tiles are staged in shared memory, radix-16
+// sub-passes run as tcgen05.mma products with TMEM accumulators, the other
+// radices on the CUDA cores in FP32.  Each persistent CTA allocates its TMEM
+// columns once and builds the DFT matrix once.
+// Shared memory: [padded tile][X hi][X lo][W hi][W lo].
+// ---------------------------------------------------------------------------
+constexpr size_t kUmmaTileBytes = 36864;  // >= pass_smem_bytes<F32>(256), 1 KB multiple
+
+inline size_t umma_smem_bytes() { return kUmmaTileBytes + 2 * kUmmaXBytes + 2 * kUmmaWBytes; }
+
+// One tile: staged load (inter-pass twiddles), the sub-passes, the store.
+template <int SG, int IN, int OUT, bool L2_ONLY>
+__device__ __forceinline__ bool umma_tile(const PassParams& p, long long tile, f2* sm, UmmaCtx& u,
+                                          int tid) {
+  using IE = typename IOElem<IN>::T;
+  long long line0, j0;
+  tile_origin(p, tile, line0, j0);
+  {
+    IE raw[kEPT];
+    load_tile_raw<IE, IN, 256, L2_ONLY>(p, line0, j0, tid, raw);
+#pragma unroll
+    for (int k = 0; k < kEPT; ++k) stage_elem<F32, SG, IN>(p, line0, j0, tid + k * 256, raw[k], sm);
+  }
+  __syncthreads();
+  const int cs = col_stride(p.logR, F32::kPadShift);
+  bool ok = true;
+  int logNsub = 0;
+  for (int k = 0; k < p.nq; ++k) {
+    switch (p.q[k]) {
+      case 4: ok = subpass16_umma<SG>(sm, p.logR, cs, logNsub, p.tw, u, tid) && ok; break;
+      case 3: subpass<F32, SG, 8>(sm, p.logR, cs, logNsub, p.tw, tid, 256); break;
+      case 2: subpass<F32, SG, 4>(sm, p.logR, cs, logNsub, p.tw, tid, 256); break;
+      default: subpass<F32, SG, 2>(sm, p.logR, cs, logNsub, p.tw, tid, 256); break;
+    }
+    logNsub += p.q[k];
+  }
+  if (ok) store_tile<F32, SG, OUT, 256>(p, line0, j0, sm, tid);
+  return ok;
+}
+
+template <int SG, int SIO>
+__global__ void __launch_bounds__(256, 2) k_batch_umma(BatchParams P) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  f2* sm = reinterpret_cast<f2*>(smem_raw);
+  unsigned char* xhi = smem_raw + kUmmaTileBytes;
+  unsigned char* whi = xhi + 2 * kUmmaXBytes;
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tslot;
+  __shared__ long long s_item;
+  __shared__ int s_ok, s_fail;
+  const int tid = threadIdx.x;
+  if (tid < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(&tslot)),
+                 "r"(kUmmaTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    s_fail = 0;
+  }
+  umma_build_w<SG>(whi, whi + kUmmaWBytes, reinterpret_cast<const f2*>(P.ranges[0].p.tw.dense),
+                   tid, 256);
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  UmmaCtx u;
+  u.xhi = xhi;
+  u.xlo = xhi + kUmmaXBytes;
+  u.xhi_s = smem_addr(u.xhi);
+  u.xlo_s = smem_addr(u.xlo);
+  u.whi_s = smem_addr(whi);
+  u.wlo_s = smem_addr(whi + kUmmaWBytes);
+  u.tmem = tslot;
+  u.bar = &bar;
+  u.phase = 0;
+  for (;;) {
+    if (tid == 0) s_item = (long long)atomicAdd(P.head, 1ull);
+    __syncthreads();
+    const long long item = s_item;
+    __syncthreads();
+    if (item >= P.total) break;
+    int ri = 0;
+    while (ri + 1 < P.nranges && item >= P.ranges[ri + 1].item0) ++ri;
+    const BatchRange& R = P.ranges[ri];
+    const PassParams& p = R.p;
+    const long long tile = item - R.item0;
+    const long long line0 = (R.kind != 0) ? (tile >> ((p.logL - p.logR) - p.logC)) : 0;
+    bool ok;
+    if (R.kind == 2) {
+      if (tid == 0) {
+        volatile unsigned int* cnt = P.done + R.first + line0;
+        unsigned int it = 0;
+        int okw = 1;
+        while (*cnt < R.need) {
+          if (++it > P.spin_limit) {
+            atomicExch(P.err, 1);
+            okw = 0;
+            break;
+          }
+          __nanosleep(128);
+        }
+        __threadfence();
+        s_ok = okw;
+      }
+      __syncthreads();
+      if (!s_ok) continue;
+      ok = umma_tile<SG, SIO, IO_D2, true>(p, tile, sm, u, tid);
+    } else if (R.kind == 1) {
+      ok = umma_tile<SG, IO_D2, SIO, false>(p, tile, sm, u, tid);
+      __threadfence();
+      __syncthreads();
+      if (tid == 0 && ok) atomicAdd(P.done + R.first + line0, 1u);
+    } else {
+      ok = umma_tile<SG, IO_D2, IO_D2, false>(p, tile, sm, u, tid);
+    }
+    if (!ok) {
+      // a wait for the tensor cores ran out: report, stop taking tiles
+      if (tid == 0) {
+        atomicExch(P.err, 1);
+        s_fail = 1;
+      }
+    }
+    __syncthreads();
+    if (s_fail) break;
+  }
+  // the products of a wait that ran out may still be in flight: wait for
+  // them (bounded) before the TMEM is freed
+  if (s_fail) mbar_wait_bounded(&bar, u.phase ^ 1u, kUmmaWaitLimit);
+  tc_fence_before();
+  __syncthreads();
+  if (tid < 32)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(u.tmem),
+                 "r"(kUmmaTmemCols)
+                 : "memory");
+}
+
+template <int SG, int SIO>
+static cudaError_t prepare_umma_t() {
+  static DeviceOnce done;
+  return smem_opt_in(k_batch_umma<SG, SIO>, umma_smem_bytes(), done);
+}
+
+template <int SG, int SIO>
+static cudaError_t launch_batch_umma_t(const BatchParams& P, int grid, cudaStream_t st) {
+  cudaError_t e = prepare_umma_t<SG, SIO>();
+  if (e != cudaSuccess) return e;
+  k_batch_umma<SG, SIO><<<grid, 256, umma_smem_bytes(), st>>>(P);
+  return cudaGetLastError();
+}
+
+template <int SG, int SIO>
+static int occupancy_umma_t() {
+  int n = 0;
+  if (prepare_umma_t<SG, SIO>() != cudaSuccess) return 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_umma<SG, SIO>, 256, umma_smem_bytes());
+  // each CTA holds kUmmaTmemCols of the SM's 512 TMEM columns
+  return n < (int)(512 / kUmmaTmemCols) ? n : (int)(512 / kUmmaTmemCols);
 }
 
 // ---------------------------------------------------------------------------

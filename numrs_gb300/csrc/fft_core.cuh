@@ -377,17 +377,16 @@ __device__ __forceinline__ void run_subpasses(const PassParams& p, typename F::S
   }
 }
 
-// The R-point DFTs of the tile's columns, then the store at the autosorted
-// positions.  Starts after a barrier that made the staged tile visible.
+// The store of a transformed tile at the autosorted positions (after the
+// barrier that ends the last sub-pass).
 template <class F, int SG, int OUT, int T>
-__device__ __forceinline__ void tile_compute_store(const PassParams& p, long long line0,
-                                                   long long j0, typename F::S* sm, int tid) {
+__device__ __forceinline__ void store_tile(const PassParams& p, long long line0, long long j0,
+                                           const typename F::S* sm, int tid) {
   using C = typename F::C;
   using OE = typename IOElem<OUT>::T;
   constexpr int sh = F::kPadShift;
   const int logR = p.logR, logC = p.logC;
   const int cs = col_stride(logR, sh);
-  run_subpasses<F, SG, T>(p, sm, cs, tid);
   if (p.out_ptrs == nullptr) {
     // linear layout: per-thread base plus the slot offsets out_off[k]
     long long ct;
@@ -423,6 +422,15 @@ __device__ __forceinline__ void tile_compute_store(const PassParams& p, long lon
     const long long jd = ((j >> p.logNs) << (p.logNs + logR)) + (j & (p.Ns - 1));
     gstore<F, OUT>(base, (jd + ((long long)r << p.logNs)) * p.s, v);
   }
+}
+
+// The R-point DFTs of the tile's columns, then the store at the autosorted
+// positions.  Starts after a barrier that made the staged tile visible.
+template <class F, int SG, int OUT, int T>
+__device__ __forceinline__ void tile_compute_store(const PassParams& p, long long line0,
+                                                   long long j0, typename F::S* sm, int tid) {
+  run_subpasses<F, SG, T>(p, sm, col_stride(p.logR, F::kPadShift), tid);
+  store_tile<F, SG, OUT, T>(p, line0, j0, sm, tid);
 }
 
 // Address of tile element e in global memory, input side, for tiles whose

@@ -192,13 +192,15 @@ cudaError_t launch_correl_direct(const double* a, const double* b, double* out, 
 cudaError_t launch_twofft_pack(const double* d1, const double* d2, double* fft1, long long n,
                                cudaStream_t st);
 cudaError_t launch_twofft_split(double* fft1, double* fft2, long long n, cudaStream_t st);
-// twofft-packed convlv/correl: z = a + i b (m > 0: b is an m-tap response,
-// expanded in wrap-around order), then after the n-point FFT the fused split,
-// product and inverse twist in place (kind as launch_spectral_product).
+// twofft-packed convlv/correl: z = a + i s b (m > 0: b is an m-tap response,
+// expanded in wrap-around order; s a power of two near |a|/|b| computed on the
+// device into sums[0..1], or 1 when sums is null), then after the n-point FFT
+// the fused split, product (undoing s) and inverse twist in place (kind as
+// launch_spectral_product; the same sums).
 cudaError_t launch_pack_pair(const double* a, const double* b, long long m, double* z, long long n,
-                             cudaStream_t st);
+                             double* sums, cudaStream_t st);
 cudaError_t launch_spectral_two(Form f, int kind, double* z, long long n, Twiddles tw,
-                                cudaStream_t st);
+                                const double* sums, cudaStream_t st);
 // rlft3 steps: speq gather (forward) and the twist along the last axis.
 cudaError_t launch_rlft3_speq(const double* data, double* speq, long long nn1, long long nn2,
                               long long nn3, cudaStream_t st);

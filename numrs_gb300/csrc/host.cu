@@ -73,6 +73,7 @@ struct Ctx {
   unsigned int dbg_spin_limit = 0;
   unsigned int dbg_need_extra = 0;
   int dbg_first_radix_delta = 0;  // shifts the default two-pass batch split
+  bool tc_umma = true;  // tensor-core batch form on tcgen05 (GBFFT_TC_UMMA=0: mma.sync)
   // convlv/correl forward transforms: 0 = the two inputs as two n/2-point
   // realft lines, 1 = packed as one n-point complex FFT (twofft)
   int spectral_path = 0;
@@ -170,6 +171,8 @@ int init_locked(int device) {
   g.tune_verbose = tv && tv[0] == '1';
   const char* tc = getenv("GBFFT_TUNE_CACHE");
   if (tc) g.tune_cache = tc;
+  const char* um = getenv("GBFFT_TC_UMMA");
+  g.tc_umma = !(um && um[0] == '0');
   g.inited = true;
   return GBFFT_OK;
 }
@@ -803,6 +806,7 @@ struct BatchPlan {
   BatchParams P;
   int grid = 0;
   bool prefetch = false;  // bulk-copy prefetching kernel
+  bool umma = false;      // tensor-core form on tcgen05 (k_batch_umma)
   bool host = false;      // the arrays are host memory, accessed directly
   cudaGraphExec_t exec = nullptr;
   long long launches_per_call = 0;
@@ -952,7 +956,11 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
   const char* pfenv = getenv("GBFFT_BATCH_PREFETCH");
   // (bulk copies are not used on host memory)
   b.prefetch = f != FORM_F64 && aligned && !host_ptrs && pfenv && pfenv[0] == '1';
-  int per = b.prefetch ? batch_pf_blocks_per_sm(f, sign) : batch_blocks_per_sm(f, sign);
+  // the tensor-core form runs its radix-16 sub-passes on tcgen05 unless
+  // GBFFT_TC_UMMA=0 selects the warp-level mma.sync kernel
+  b.umma = f == FORM_TC32 && !b.prefetch && g.tc_umma;
+  int per = b.prefetch ? batch_pf_blocks_per_sm(f, sign)
+                       : (b.umma ? batch_blocks_per_sm_umma(sign) : batch_blocks_per_sm(f, sign));
   if (tune && tune->per > 0 && tune->per < per) per = tune->per;
   if (per < 1) per = 1;
   b.grid = (int)std::min<long long>((long long)dev_sms * per, std::max<long long>(item, 1));
@@ -964,7 +972,8 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
   cudaError_t le = cudaSuccess;
   if (item > 0)
     le = b.prefetch ? launch_batch_pf(f, sign, b.P, b.grid, g.stream)
-                    : launch_batch(f, sign, b.P, b.grid, g.stream);
+                    : (b.umma ? launch_batch_umma(sign, b.P, b.grid, g.stream)
+                              : launch_batch(f, sign, b.P, b.grid, g.stream));
   cudaError_t ce = cudaStreamEndCapture(g.stream, &graph);
   if (le != cudaSuccess || ce != cudaSuccess) {
     if (graph) cudaGraphDestroy(graph);
@@ -1118,7 +1127,8 @@ BatchTune tune_batch(Form f, int sign, const size_t* nn, size_t count) {
     }
     best.first_radix[L] = keep;
   }
-  const int occ = batch_blocks_per_sm(f, sign);
+  const int occ = (f == FORM_TC32 && g.tc_umma) ? batch_blocks_per_sm_umma(sign)
+                                                 : batch_blocks_per_sm(f, sign);
   for (int per = occ - 1; per >= 1 && per >= occ - 2; --per) {
     BatchTune t = best;
     t.per = per;
@@ -1759,12 +1769,19 @@ static int spectral_twofft(const Call& c, int kind, const double* a, const doubl
     da = in;
     db = in + n;
   }
-  CK(launch_pack_pair(da, db, kind == 2 ? 0 : (long long)m, z, (long long)n, g.cur));
-  g.launches++;
+  // the packed imaginary part is scaled to the real part's magnitude (not for
+  // deconvolution, whose |R|^2 threshold is absolute)
+  double* sums = nullptr;
+  if (kind != 1) {
+    TRY(ensure(g.ptrtab, 64));
+    sums = (double*)g.ptrtab.p;
+  }
+  CK(launch_pack_pair(da, db, kind == 2 ? 0 : (long long)m, z, (long long)n, sums, g.cur));
+  g.launches += sums ? 2 : 1;
   TRY(run_axis(f, 1, axis_plan((long long)n, 1, 1, 0, (long long)n, f), z));
   {
     ProfScope ps(PK_SPECTRAL, 3.0 * n * 8);
-    CK(launch_spectral_two(f, kind, z, (long long)n, tw, g.cur));
+    CK(launch_spectral_two(f, kind, z, (long long)n, tw, sums, g.cur));
   }
   g.launches++;
   const long long nh = (long long)n / 2;

@@ -450,11 +450,47 @@ cudaError_t launch_twofft_pack(const double* d1, const double* d2v, double* fft1
 // src/Correlation.rs:53-55): the two real inputs travel as the real and
 // imaginary parts of one n-point complex FFT.
 // ---------------------------------------------------------------------------
-// z_j = a_j + i b_j.  With m > 0, b is an m-tap response in wrap-around order
-// (Numerical Recipes convlv contract) expanded on the fly to n values.
-__global__ void k_pack_pair(const double* a, const double* b, long long m, double* z,
-                            long long n) {
+// The two inputs' sums of squares (b: its nb stored values), one block, a
+// fixed reduction order: sums[0] = |a|^2, sums[1] = |b|^2.
+__global__ void k_sumsq_pair(const double* a, long long na, const double* b, long long nb,
+                             double* sums) {
+  __shared__ double red[2][256];
+  double sa = 0.0, sb = 0.0;
+  for (long long i = threadIdx.x; i < na; i += blockDim.x) sa += a[i] * a[i];
+  for (long long i = threadIdx.x; i < nb; i += blockDim.x) sb += b[i] * b[i];
+  red[0][threadIdx.x] = sa;
+  red[1][threadIdx.x] = sb;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + w];
+      red[1][threadIdx.x] += red[1][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    sums[0] = red[0][0];
+    sums[1] = red[1][0];
+  }
+}
+
+// Power of two s near |a| / |b|: the packed imaginary part s b then has the
+// real part's magnitude, so that the rounding of the shared transform (relative
+// to the larger input) does not swamp the smaller input's spectrum.  Exact in
+// every form; 1 when either input is zero.
+__device__ __forceinline__ double pack_scale(const double* sums) {
+  if (!sums || !(sums[0] > 0.0) || !(sums[1] > 0.0)) return 1.0;
+  int e = (int)rint(0.5 * log2(sums[0] / sums[1]));
+  e = e > 600 ? 600 : (e < -600 ? -600 : e);
+  return ldexp(1.0, e);
+}
+
+// z_j = a_j + i s b_j.  With m > 0, b is an m-tap response in wrap-around
+// order (Numerical Recipes convlv contract) expanded on the fly to n values.
+__global__ void k_pack_pair(const double* a, const double* b, long long m, double* z, long long n,
+                            const double* sums) {
   const long long half = (m - 1) / 2;
+  const double sc = pack_scale(sums);
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
        j += (long long)gridDim.x * blockDim.x) {
     double v;
@@ -462,16 +498,17 @@ __global__ void k_pack_pair(const double* a, const double* b, long long m, doubl
     else if (half > 0 && j >= n - half) v = b[m - (n - j)];
     else if (j < (m + 1) / 2) v = b[j];
     else v = 0.0;
-    reinterpret_cast<d2*>(z)[j] = d2{a[j], v};
+    reinterpret_cast<d2*>(z)[j] = d2{a[j], sc * v};
   }
 }
 
 cudaError_t launch_pack_pair(const double* a, const double* b, long long m, double* z, long long n,
-                             cudaStream_t st) {
+                             double* sums, cudaStream_t st) {
+  if (sums) k_sumsq_pair<<<1, 256, 0, st>>>(a, n, b, m > 0 ? m : n, sums);
   int blocks = (int)((n + 255) / 256);
   if (blocks > 152 * 8) blocks = 152 * 8;
   if (blocks < 1) blocks = 1;
-  k_pack_pair<<<blocks, 256, 0, st>>>(a, b, m, z, n);
+  k_pack_pair<<<blocks, 256, 0, st>>>(a, b, m, z, n, sums);
   return cudaGetLastError();
 }
 
@@ -483,10 +520,12 @@ cudaError_t launch_pack_pair(const double* a, const double* b, long long m, doub
 // of Z is read by one thread only, the one that writes it, so the step runs
 // in place.
 template <class F, int KIND>
-__global__ void k_spectral_two(double* z, long long n, Twiddles tw) {
+__global__ void k_spectral_two(double* z, long long n, Twiddles tw, const double* sums) {
   using C = typename F::C;
   const long long nh = n / 2, nq = n / 4;
-  const double inv_no2 = 2.0 / (double)n;
+  // B was packed as s b: the products take 1/s (deconvolution is packed
+  // unscaled, sums = nullptr, so that its |B|^2 threshold keeps its meaning)
+  const double inv_no2 = (2.0 / (double)n) / pack_scale(sums);
   const int logn = 63 - __clzll(n);
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k <= nq;
        k += (long long)gridDim.x * blockDim.x) {
@@ -522,15 +561,15 @@ __global__ void k_spectral_two(double* z, long long n, Twiddles tw) {
 }
 
 cudaError_t launch_spectral_two(Form f, int kind, double* z, long long n, Twiddles tw,
-                                cudaStream_t st) {
+                                const double* sums, cudaStream_t st) {
   long long work = n / 4 + 1;
   int blocks = (int)((work + 255) / 256);
   if (blocks > 152 * 16) blocks = 152 * 16;
-#define SP2_LAUNCH(FT)                                                        \
-  switch (kind) {                                                             \
-    case 0: k_spectral_two<FT, 0><<<blocks, 256, 0, st>>>(z, n, tw); break;   \
-    case 1: k_spectral_two<FT, 1><<<blocks, 256, 0, st>>>(z, n, tw); break;   \
-    default: k_spectral_two<FT, 2><<<blocks, 256, 0, st>>>(z, n, tw); break;  \
+#define SP2_LAUNCH(FT)                                                              \
+  switch (kind) {                                                                   \
+    case 0: k_spectral_two<FT, 0><<<blocks, 256, 0, st>>>(z, n, tw, sums); break;   \
+    case 1: k_spectral_two<FT, 1><<<blocks, 256, 0, st>>>(z, n, tw, sums); break;   \
+    default: k_spectral_two<FT, 2><<<blocks, 256, 0, st>>>(z, n, tw, sums); break;  \
   }
   if (f == FORM_F64) { SP2_LAUNCH(F64) }
   else if (f == FORM_F32 || f == FORM_TC32) { SP2_LAUNCH(F32) }
