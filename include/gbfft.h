@@ -113,13 +113,19 @@ long long gbfft_launch_count(int reset);
  *                                 batch launch's two-pass bins away from
  *                                 half the length (the splits the autotuner
  *                                 tries), so tests can check each one
+ *   GBFFT_DEBUG_FUSED_TWIST       0: realft runs its twist as a kernel of its
+ *                                 own instead of on a pass (1, the default)
+ *   GBFFT_DEBUG_TC_UMMA           1: the tensor-core batch form on tcgen05
+ *                                 (also GBFFT_TC_UMMA=1), 0: on mma.sync
  * The batch settings drop the cached batch plan.  Nothing here hangs or
  * faults a GPU: every device wait stays bounded. */
 enum {
   GBFFT_DEBUG_FAIL_ALLOC_AT = 1,
   GBFFT_DEBUG_BATCH_SPIN_LIMIT = 2,
   GBFFT_DEBUG_BATCH_NEED_EXTRA = 3,
-  GBFFT_DEBUG_BATCH_FIRST_RADIX_DELTA = 4
+  GBFFT_DEBUG_BATCH_FIRST_RADIX_DELTA = 4,
+  GBFFT_DEBUG_FUSED_TWIST = 5,
+  GBFFT_DEBUG_TC_UMMA = 6
 };
 int gbfft_debug_set(int key, long long value);
 int gbfft_profile(int enable);  /* also clears the records */

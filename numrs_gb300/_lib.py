@@ -70,6 +70,8 @@ DEBUG_FAIL_ALLOC_AT = 1
 DEBUG_BATCH_SPIN_LIMIT = 2
 DEBUG_BATCH_NEED_EXTRA = 3
 DEBUG_BATCH_FIRST_RADIX_DELTA = 4
+DEBUG_FUSED_TWIST = 5
+DEBUG_TC_UMMA = 6
 
 _lib = None
 

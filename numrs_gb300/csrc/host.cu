@@ -73,7 +73,10 @@ struct Ctx {
   unsigned int dbg_spin_limit = 0;
   unsigned int dbg_need_extra = 0;
   int dbg_first_radix_delta = 0;  // shifts the default two-pass batch split
-  bool tc_umma = true;  // tensor-core batch form on tcgen05 (GBFFT_TC_UMMA=0: mma.sync)
+  // tensor-core batch form on tcgen05 (GBFFT_TC_UMMA=1) instead of the
+  // warp-level mma.sync kernel; measured slower on the batch, so off by default
+  bool tc_umma = false;
+  bool fused_twist = true;  // realft twist on a pass (off: its own kernel)
   // convlv/correl forward transforms: 0 = the two inputs as two n/2-point
   // realft lines, 1 = packed as one n-point complex FFT (twofft)
   int spectral_path = 0;
@@ -172,7 +175,7 @@ int init_locked(int device) {
   const char* tc = getenv("GBFFT_TUNE_CACHE");
   if (tc) g.tune_cache = tc;
   const char* um = getenv("GBFFT_TC_UMMA");
-  g.tc_umma = !(um && um[0] == '0');
+  g.tc_umma = um && um[0] == '1';
   g.inited = true;
   return GBFFT_OK;
 }
@@ -708,7 +711,7 @@ int realft_dev(Form f, double* d, long long n, int isign, long long batch = 1,
   Twiddles tw;
   TRY(tables(f, tw));
   const long long nh = n / 2;
-  if (nh >= 2) {
+  if (nh >= 2 && g.fused_twist) {
     // the twist rides on the last pass of the forward FFT or the first pass
     // of the inverse one: no pass of its own over the data
     const AxisPlan& ap = axis_plan(nh, 1, batch, 0, dist / 2, f);
@@ -956,8 +959,8 @@ int build_batch_plan(BatchPlan& b, Form f, int sign, double* const* dptrs, const
   const char* pfenv = getenv("GBFFT_BATCH_PREFETCH");
   // (bulk copies are not used on host memory)
   b.prefetch = f != FORM_F64 && aligned && !host_ptrs && pfenv && pfenv[0] == '1';
-  // the tensor-core form runs its radix-16 sub-passes on tcgen05 unless
-  // GBFFT_TC_UMMA=0 selects the warp-level mma.sync kernel
+  // the tensor-core form runs its radix-16 sub-passes on tcgen05 when
+  // selected (GBFFT_TC_UMMA=1), else on the warp-level mma.sync kernel
   b.umma = f == FORM_TC32 && !b.prefetch && g.tc_umma;
   int per = b.prefetch ? batch_pf_blocks_per_sm(f, sign)
                        : (b.umma ? batch_blocks_per_sm_umma(sign) : batch_blocks_per_sm(f, sign));
@@ -1351,6 +1354,13 @@ int gbfft_debug_set(int key, long long value) {
       if (value < 0) return fail(GBFFT_INVALID_ARG, "debug_set: negative allocation index");
       g.fail_alloc_at = value;
       g.alloc_calls = 0;
+      return GBFFT_OK;
+    case GBFFT_DEBUG_FUSED_TWIST:
+      g.fused_twist = value != 0;
+      return GBFFT_OK;
+    case GBFFT_DEBUG_TC_UMMA:
+      g.tc_umma = value != 0;
+      batch_plan_free(g_batch);
       return GBFFT_OK;
     case GBFFT_DEBUG_BATCH_FIRST_RADIX_DELTA:
       if (value < -12 || value > 12) return fail(GBFFT_INVALID_ARG, "debug_set: value out of range");
