@@ -18,6 +18,8 @@
 // reports GBFFT_TIMEOUT.  A pass-2 tile only ever waits on tiles that were
 // handed out before it, so the wait always ends unless a CTA died.
 #pragma once
+#include <cstdio>
+#include <cstdlib>
 #include "fft_core.cuh"
 #include "batch.h"
 #include "tma.cuh"
@@ -236,8 +238,17 @@ static cudaError_t launch_batch_umma_t(const BatchParams& P, int grid, cudaStrea
 template <int SG, int SIO>
 static int occupancy_umma_t() {
   int n = 0;
-  if (prepare_umma_t<SG, SIO>() != cudaSuccess) return 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_umma<SG, SIO>, 256, umma_smem_bytes());
+  cudaError_t e = prepare_umma_t<SG, SIO>();
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_umma<SG, SIO>, 256,
+                                                      umma_smem_bytes());
+  if (getenv("GBFFT_TUNE_VERBOSE"))
+    fprintf(stderr, "gbfft k_batch_umma: %d CTAs per SM (%s), %zu B dynamic shared memory\n", n,
+            cudaGetErrorString(e), umma_smem_bytes());
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
   // each CTA holds kUmmaTmemCols of the SM's 512 TMEM columns
   return n < (int)(512 / kUmmaTmemCols) ? n : (int)(512 / kUmmaTmemCols);
 }

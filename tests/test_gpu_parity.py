@@ -395,7 +395,22 @@ def test_sine_cosine_transforms(nr, form, n):
             if kind == "sinft":
                 y0[0] = 0.0
             exact = _exact_trig(kind, y0, n, isign or 1)
-            assert_fp64_close(d, exact, log2n, what + " vs exact " + form)
+            if kind == "cosft2" and isign == -1:
+                # The inverse divides by 2 sin(pi (2i+1)/(4n)) (k_cosft2_inv_post;
+                # the crate's inverse_transform, src/Cos_FT2.rs:89-173, does the
+                # same), which multiplies one rounding of its inputs by up to
+                # 0.5/sin(pi/(4n)) (6.7e5 at n = 2^20) at the two ends.  The
+                # max-abs bar adds that conditioning, element by element.
+                e = rel_l2(d, exact)
+                assert e <= 1e-12, "%s rel-L2 %.3e" % (what, e)
+                i = np.arange(n)
+                kappa = 0.5 / np.sin(np.pi * (2 * np.minimum(i, n - 1 - i) + 1) / (4 * n))
+                amax = np.abs(exact).max()
+                bound = 1e-12 * amax * log2n + 8 * 2.2e-16 * kappa * amax * log2n
+                worst = int(np.argmax(np.abs(d - exact) / bound))
+                assert np.abs(d[worst] - exact[worst]) <= bound[worst], "%s at %d" % (what, worst)
+            else:
+                assert_fp64_close(d, exact, log2n, what + " vs exact " + form)
             drift = rel_l2(ref, exact)
             assert rel_l2(d, ref) <= drift + 1e-12, what
 
