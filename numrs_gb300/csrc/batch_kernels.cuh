@@ -91,33 +91,48 @@ constexpr size_t kUmmaTileBytes = 36864;  // >= pass_smem_bytes<F32>(256), 1 KB 
 
 inline size_t umma_smem_bytes() { return kUmmaTileBytes + 2 * kUmmaXBytes + 2 * kUmmaWBytes; }
 
-// One tile: staged load (inter-pass twiddles), the sub-passes, the store.
+// One tile, fused as the mma.sync kernel's tiles are: the first sub-pass reads
+// global memory and the last one writes it; radix-16 sub-passes run as
+// tcgen05 products, the other radices on the CUDA cores in FP32.  A pass of a
+// single sub-pass runs on the CUDA cores from global to global.
 template <int SG, int IN, int OUT, bool L2_ONLY>
 __device__ __forceinline__ bool umma_tile(const PassParams& p, long long tile, f2* sm, UmmaCtx& u,
                                           int tid) {
-  using IE = typename IOElem<IN>::T;
   long long line0, j0;
   tile_origin(p, tile, line0, j0);
-  {
-    IE raw[kEPT];
-    load_tile_raw<IE, IN, 256, L2_ONLY>(p, line0, j0, tid, raw);
-#pragma unroll
-    for (int k = 0; k < kEPT; ++k) stage_elem<F32, SG, IN>(p, line0, j0, tid + k * 256, raw[k], sm);
+  if (p.nq == 1) {
+    switch (p.q[0]) {
+      case 4: only_subpass<TC32, SG, IN, OUT, 16, 256, L2_ONLY>(p, line0, j0, tid); break;
+      case 3: only_subpass<TC32, SG, IN, OUT, 8, 256, L2_ONLY>(p, line0, j0, tid); break;
+      case 2: only_subpass<TC32, SG, IN, OUT, 4, 256, L2_ONLY>(p, line0, j0, tid); break;
+      default: only_subpass<TC32, SG, IN, OUT, 2, 256, L2_ONLY>(p, line0, j0, tid); break;
+    }
+    return true;
   }
-  __syncthreads();
   const int cs = col_stride(p.logR, F32::kPadShift);
   bool ok = true;
-  int logNsub = 0;
-  for (int k = 0; k < p.nq; ++k) {
+  if (p.q[0] == 4) {
+    ok = subpass16_umma<SG, 1, 0, IN, OUT, L2_ONLY>(p, line0, j0, sm, cs, 0, u, tid);
+  } else {
+    first_subpass_q<TC32, SG, IN, 256, L2_ONLY>(p.q[0], p, line0, j0, sm, cs, tid);
+    __syncthreads();
+  }
+  int logNsub = p.q[0];
+  for (int k = 1; k + 1 < p.nq; ++k) {
     switch (p.q[k]) {
-      case 4: ok = subpass16_umma<SG>(sm, p.logR, cs, logNsub, p.tw, u, tid) && ok; break;
+      case 4:
+        ok = subpass16_umma<SG, 0, 0, IN, OUT, L2_ONLY>(p, line0, j0, sm, cs, logNsub, u, tid) && ok;
+        break;
       case 3: subpass<F32, SG, 8>(sm, p.logR, cs, logNsub, p.tw, tid, 256); break;
       case 2: subpass<F32, SG, 4>(sm, p.logR, cs, logNsub, p.tw, tid, 256); break;
       default: subpass<F32, SG, 2>(sm, p.logR, cs, logNsub, p.tw, tid, 256); break;
     }
     logNsub += p.q[k];
   }
-  if (ok) store_tile<F32, SG, OUT, 256>(p, line0, j0, sm, tid);
+  if (p.q[p.nq - 1] == 4)
+    ok = subpass16_umma<SG, 0, 1, IN, OUT, L2_ONLY>(p, line0, j0, sm, cs, logNsub, u, tid) && ok;
+  else
+    last_subpass_q<TC32, SG, OUT, 256>(p.q[p.nq - 1], p, line0, j0, sm, cs, tid);
   return ok;
 }
 
@@ -224,7 +239,20 @@ __global__ void __launch_bounds__(256, 2) k_batch_umma(BatchParams P) {
 template <int SG, int SIO>
 static cudaError_t prepare_umma_t() {
   static DeviceOnce done;
-  return smem_opt_in(k_batch_umma<SG, SIO>, umma_smem_bytes(), done);
+  static DeviceOnce carveout;
+  cudaError_t e = smem_opt_in(k_batch_umma<SG, SIO>, umma_smem_bytes(), done);
+  if (e != cudaSuccess) return e;
+  // two CTAs of 108 KB need the largest shared-memory configuration of the
+  // SM; without the preference the occupancy (and the launch) assume one
+  int dev = 0;
+  e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (carveout.bits.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(k_batch_umma<SG, SIO>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared);
+  if (e == cudaSuccess && bit) carveout.bits.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
 }
 
 template <int SG, int SIO>

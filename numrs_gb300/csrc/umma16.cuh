@@ -136,49 +136,94 @@ __device__ __forceinline__ void umma_build_w(unsigned char* whi, unsigned char* 
 }
 
 // One radix-16 Stockham sub-pass of a 4096-point tile (256 threads, one
-// butterfly each; layout and index rules as subpass<F, SG, 16>).  Starts
-// after a barrier that made the tile visible, ends with one.  Returns false
-// when the wait for the products ran out (the tile's outputs are then not
-// written).
-template <int SG>
-__device__ __forceinline__ bool subpass16_umma(f2* sm, int logR, int cs, int logNs,
-                                               const Twiddles& tw, UmmaCtx& u, int tid) {
+// butterfly each; layout and index rules as subpass<F, SG, 16>).  SRC = 0 takes
+// the inputs from the shared tile (sub-pass twiddles of level 16 Ns); SRC = 1
+// is a pass's first sub-pass and loads them straight from global memory with
+// the pass's inter-pass twiddles.  DST = 0 writes the outputs into the tile;
+// DST = 1 is a pass's last sub-pass and stores them straight from TMEM to
+// global memory.  Butterfly b of the X rows is (column, row) =
+// butterfly_cj(b) with the global side's contiguity when a side is global, so
+// that lanes of a warp stay coalesced.  Starts after a barrier that made the
+// tile visible, ends with one.  Returns false when the wait for the products
+// ran out (the outputs are then not written).
+template <int SG, int SRC, int DST, int IN, int OUT, bool L2_ONLY>
+__device__ __forceinline__ bool subpass16_umma(const PassParams& p, long long line0, long long j0,
+                                               f2* sm, int cs, int logNs, UmmaCtx& u, int tid) {
+  using IE = typename IOElem<IN>::T;
+  using OE = typename IOElem<OUT>::T;
   constexpr int sh = 5;  // FP32 shared-memory padding (F32::kPadShift)
+  const int logR = p.logR;
   const int logRQ = logR - 4, RQ = 1 << logRQ, Ns = 1 << logNs;
-  const f2* twd = reinterpret_cast<const f2*>(tw.dense);
+  const f2* twd = reinterpret_cast<const f2*>(p.tw.dense);
+  const long long rem = (p.mode == 0) ? (1ll << 62) : p.nlines - line0;
+  // the butterfly of X row b
+  auto cj = [&](int b, int& c, int& j) {
+    if (SRC == 1) butterfly_cj(b, p.in_rcontig, logRQ, p.logC, c, j);
+    else if (DST == 1) butterfly_cj(b, p.out_rcontig, logRQ, p.logC, c, j);
+    else { c = b >> logRQ; j = b & (RQ - 1); }
+  };
   {
-    // this thread's butterfly: inputs, twiddles, hi/lo split, row of X
     const int b = tid;
-    const int c = b >> logRQ, j = b & (RQ - 1), jm = j & (Ns - 1);
-    const int cb = c * cs;
-    uint32_t hre[16], lre[16], him[16], lim[16];
+    int c, j;
+    cj(b, c, j);
+    float xr[16], xi[16];
+    if (SRC == 1) {
+      // inputs from global memory; inter-pass twiddles w^(jm (j + t R/16))
+      const long long rs = (p.L >> logR) * p.s;
+      const long long step = rs << logRQ;
+      IE raw[16];
+      if (c < rem) {
+        const IE* src = col_src<IN>(p, line0, j0, c) + j * rs;
 #pragma unroll
-    for (int t = 0; t < 16; ++t) {
-      f2 v = sm[cb + pidx(j + t * RQ, sh)];
-      if (logNs > 0 && jm != 0 && t != 0) {
-        const f2 w = twd[(1 << (logNs + 4)) + ((jm * t) & ((Ns << 4) - 1))];
-        const float wy = SG > 0 ? w.y : -w.y;
-        const float re = fmaf(v.x, w.x, -v.y * wy);
-        const float im = fmaf(v.x, wy, v.y * w.x);
-        v.x = re;
-        v.y = im;
+        for (int t = 0; t < 16; ++t) load_elem<IE, L2_ONLY>(src + t * step, raw[t]);
+      } else {
+#pragma unroll
+        for (int t = 0; t < 16; ++t) memset(&raw[t], 0, sizeof(IE));
       }
-      hre[t] = tf32_bits(v.x);
-      lre[t] = tf32_bits(v.x - __uint_as_float(hre[t]));
-      him[t] = tf32_bits(v.y);
-      lim[t] = tf32_bits(v.y - __uint_as_float(him[t]));
+      const long long jg = (p.mode == 0) ? j0 + c : j0;
+      const unsigned jm = (unsigned)(jg & (p.Ns - 1));
+      const int logS = p.logNs + logR;
+#pragma unroll
+      for (int t = 0; t < 16; ++t) {
+        F32::C v = gload<F32, IN>(&raw[t], 0);
+        const unsigned r = (unsigned)(j + (t << logRQ));
+        if (p.logNs > 0 && jm != 0 && r != 0) v = F32::mul(v, twiddle<F32>(p.tw, logS, jm * r, SG));
+        xr[t] = v.x;
+        xi[t] = v.y;
+      }
+    } else {
+      const int cb = c * cs, jm = j & (Ns - 1);
+#pragma unroll
+      for (int t = 0; t < 16; ++t) {
+        f2 v = sm[cb + pidx(j + t * RQ, sh)];
+        if (logNs > 0 && jm != 0 && t != 0) {
+          const f2 w = twd[(1 << (logNs + 4)) + ((jm * t) & ((Ns << 4) - 1))];
+          const float wy = SG > 0 ? w.y : -w.y;
+          const float re = fmaf(v.x, w.x, -v.y * wy);
+          const float im = fmaf(v.x, wy, v.y * w.x);
+          v.x = re;
+          v.y = im;
+        }
+        xr[t] = v.x;
+        xi[t] = v.y;
+      }
     }
+    // hi/lo split into row b of X
     const uint32_t row = (uint32_t)(b >> 7) * kUmmaXBlock + umma_off(b & 127, 0);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      *reinterpret_cast<uint4*>(u.xhi + row + q * 128) =
-          make_uint4(hre[4 * q], hre[4 * q + 1], hre[4 * q + 2], hre[4 * q + 3]);
-      *reinterpret_cast<uint4*>(u.xhi + row + (q + 4) * 128) =
-          make_uint4(him[4 * q], him[4 * q + 1], him[4 * q + 2], him[4 * q + 3]);
-      *reinterpret_cast<uint4*>(u.xlo + row + q * 128) =
-          make_uint4(lre[4 * q], lre[4 * q + 1], lre[4 * q + 2], lre[4 * q + 3]);
-      *reinterpret_cast<uint4*>(u.xlo + row + (q + 4) * 128) =
-          make_uint4(lim[4 * q], lim[4 * q + 1], lim[4 * q + 2], lim[4 * q + 3]);
+      uint32_t h[4], l[4], hh[4], ll[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        h[i] = tf32_bits(xr[4 * q + i]);
+        l[i] = tf32_bits(xr[4 * q + i] - __uint_as_float(h[i]));
+        hh[i] = tf32_bits(xi[4 * q + i]);
+        ll[i] = tf32_bits(xi[4 * q + i] - __uint_as_float(hh[i]));
+      }
+      *reinterpret_cast<uint4*>(u.xhi + row + q * 128) = make_uint4(h[0], h[1], h[2], h[3]);
+      *reinterpret_cast<uint4*>(u.xlo + row + q * 128) = make_uint4(l[0], l[1], l[2], l[3]);
+      *reinterpret_cast<uint4*>(u.xhi + row + (q + 4) * 128) = make_uint4(hh[0], hh[1], hh[2], hh[3]);
+      *reinterpret_cast<uint4*>(u.xlo + row + (q + 4) * 128) = make_uint4(ll[0], ll[1], ll[2], ll[3]);
     }
   }
   // the operands' generic-proxy writes before the tensor cores read them
@@ -221,11 +266,27 @@ __device__ __forceinline__ bool subpass16_umma(f2* sm, int logR, int cs, int log
 #pragma unroll
     for (int i = 0; i < 32; ++i) y[i] = y[i] + (s2[i] + t[i]);
     const int b2 = (warp >> 2) * 128 + (warp & 3) * 32 + lane;
-    const int c2 = b2 >> logRQ, j2 = b2 & (RQ - 1);
-    const int ob = c2 * cs;
-    const int orow = ((j2 >> logNs) << (logNs + 4)) + (j2 & (Ns - 1));
+    int c2, j2;
+    cj(b2, c2, j2);
+    if (DST == 1) {
+      // last sub-pass (Ns = R/16): outputs k at rows j + k R/16 of the column
+      if (c2 < rem) {
+        const long long rs = p.Ns * p.s;
+        const long long step = rs << logRQ;
+        OE* dst = col_dst<OUT>(p, line0, j0, c2) + j2 * rs;
 #pragma unroll
-    for (int k = 0; k < 16; ++k) sm[ob + pidx(orow + k * Ns, sh)] = f2{y[k], y[16 + k]};
+        for (int k = 0; k < 16; ++k) {
+          F32::C w = {y[k], y[16 + k]};
+          if (p.do_scale) w = apply_scale<F32>(w, p);
+          gstore<F32, OUT>(dst, k * step, w);
+        }
+      }
+    } else {
+      const int ob = c2 * cs;
+      const int orow = ((j2 >> logNs) << (logNs + 4)) + (j2 & (Ns - 1));
+#pragma unroll
+      for (int k = 0; k < 16; ++k) sm[ob + pidx(orow + k * Ns, sh)] = f2{y[k], y[16 + k]};
+    }
   }
   tc_fence_before();
   __syncthreads();
