@@ -75,7 +75,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large",
-                    choices=["large", "convlv", "four1", "batch", "fourn", "rlft3", "c1", "convbatch"])
+                    choices=["large", "convlv", "four1", "batch", "fourn", "rlft3", "c1", "convbatch",
+                             "peaks"])
     ap.add_argument("--form", default="fp64", choices=["fp64", "df64", "fp32", "tc32"])
     ap.add_argument("--no-forms", action="store_true", help="skip the extra precision forms")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched target in the default line")
@@ -1069,6 +1070,49 @@ def run_c1(args, world, rank, local):
                          "accuracy": {"roundtrip_rel_l2": err}})
 
 
+def run_peaks(args, world, rank, local):
+    """Arithmetic ceilings behind `compute_roofline`: FP64 and FP32 (TF32 off)
+    GEMM throughput through torch's cuBLAS call, timed with CUDA events.  A
+    DGEMM keeps the FP64 pipe at its DFMA rate; an SGEMM without TF32 keeps
+    the FP32 pipe at its FFMA rate.  Not an FFT workload."""
+    import torch
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    res = {}
+    try:
+        for name, dt, n, steps in (("fp64", torch.float64, 4096, 10), ("fp32", torch.float32, 8192, 20)):
+            g = torch.Generator(device=dev)
+            g.manual_seed(7)
+            a = torch.randn(n, n, dtype=dt, device=dev, generator=g)
+            b = torch.randn(n, n, dtype=dt, device=dev, generator=g)
+            c = torch.empty_like(a)
+            for _ in range(max(args.warmup, 3)):
+                torch.matmul(a, b, out=c)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(steps):
+                torch.matmul(a, b, out=c)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            res[name] = {"tflops": 2.0 * n ** 3 / ms / 1e9, "ms_per_gemm": ms, "n": n, "gemms": steps}
+            del a, b, c
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+    if rank != 0:
+        return None
+    return {"metric": "GEMM TFLOP/s (FP64 and FP32 pipe ceilings)", "value": res["fp64"]["tflops"],
+            "unit": "TFLOP/s", "n_gpus": world, "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic (seeded N(0,1) matrices)",
+            "config": {"workload": "torch.matmul square GEMMs: f64 4096^3 and f32 8192^3, TF32 off"},
+            "gemm": res, "used_in_bench": {"fp64_peak_tflops": FP64_PEAK_TFLOPS,
+                                            "fp32_peak_tflops": FP32_PEAK_TFLOPS}}
+
+
 def run_convbatch(args, world, rank, local):
     """convlv_batch: 64 convolutions of N=2^16 reals with one 257-tap response
     (the C2 response construction at N=2^16), one library call per step; the
@@ -1140,7 +1184,8 @@ def main():
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     fn = {"large": run_large, "four1": run_four1, "batch": run_batch, "fourn": run_nd,
-          "rlft3": run_nd, "c1": run_c1, "convbatch": run_convbatch}.get(args.workload)
+          "rlft3": run_nd, "c1": run_c1, "convbatch": run_convbatch,
+          "peaks": run_peaks}.get(args.workload)
     if fn is None:
         run_convlv(args, world, rank, local)
     else:

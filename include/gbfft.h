@@ -116,7 +116,8 @@ long long gbfft_launch_count(int reset);
  *   GBFFT_DEBUG_FUSED_TWIST       0: realft runs its twist as a kernel of its
  *                                 own instead of on a pass (1, the default)
  *   GBFFT_DEBUG_TC_UMMA           1: the tensor-core batch form on tcgen05
- *                                 (also GBFFT_TC_UMMA=1), 0: on mma.sync
+ *                                 (the default), 0: on mma.sync (also
+ *                                 GBFFT_TC_UMMA=0 at start-up)
  * The batch settings drop the cached batch plan.  Nothing here hangs or
  * faults a GPU: every device wait stays bounded. */
 enum {

@@ -270,13 +270,35 @@ static int occupancy_umma_t() {
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_umma<SG, SIO>, 256,
                                                       umma_smem_bytes());
+  // The occupancy query has been seen to report one CTA where the launch
+  // fits two (registers and shared memory both allow two, by the kernel's
+  // attributes and by the hardware's own occupancy limits).  Count from the
+  // attributes as well and take the larger figure when both resources fit.
+  int fit = 0;
+  if (e == cudaSuccess) {
+    cudaFuncAttributes fa;
+    cudaDeviceProp dp;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaFuncGetAttributes(&fa, k_batch_umma<SG, SIO>) == cudaSuccess &&
+        cudaGetDeviceProperties(&dp, dev) == cudaSuccess) {
+      const size_t per_cta = umma_smem_bytes() + fa.sharedSizeBytes + dp.reservedSharedMemPerBlock;
+      const int by_smem = (int)(dp.sharedMemPerMultiprocessor / per_cta);
+      const int by_regs = fa.numRegs > 0 ? dp.regsPerMultiprocessor / (fa.numRegs * 256) : 0;
+      fit = by_smem < by_regs ? by_smem : by_regs;
+    }
+    cudaGetLastError();
+  }
   if (getenv("GBFFT_TUNE_VERBOSE"))
-    fprintf(stderr, "gbfft k_batch_umma: %d CTAs per SM (%s), %zu B dynamic shared memory\n", n,
-            cudaGetErrorString(e), umma_smem_bytes());
+    fprintf(stderr,
+            "gbfft k_batch_umma: %d CTAs per SM by the occupancy query (%s), %d by the kernel's "
+            "attributes, %zu B dynamic shared memory\n",
+            n, cudaGetErrorString(e), fit, umma_smem_bytes());
   if (e != cudaSuccess) {
     cudaGetLastError();
     return 1;
   }
+  if (fit > n) n = fit;
   // each CTA holds kUmmaTmemCols of the SM's 512 TMEM columns
   return n < (int)(512 / kUmmaTmemCols) ? n : (int)(512 / kUmmaTmemCols);
 }

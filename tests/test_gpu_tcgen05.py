@@ -1,5 +1,6 @@
 """The tensor-core batch form on tcgen05 (k_batch_umma: radix-16 sub-passes as
-tcgen05.mma products with TMEM accumulators), selected in process with the
+tcgen05.mma products with TMEM accumulators, the default) and on the
+warp-level mma.sync kernel, each selected in process with the
 GBFFT_DEBUG_TC_UMMA key.  Each transform must match the oracle within the
 FP32-form bar (rel-L2 1e-6), in both directions, for single-pass bins and for
 the two-pass bins whose pass-2 tiles wait on pass-1 counters."""
@@ -11,17 +12,17 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def env():
+@pytest.fixture(scope="module", params=[1, 0], ids=["tcgen05", "mma_sync"])
+def env(request):
     pytest.importorskip("torch")
     import numrs_gb300 as nr
     from numrs_gb300 import _lib as L
     from numrs_gb300 import build
     build.build()
     lib = L.load()
-    assert lib.gbfft_debug_set(L.DEBUG_TC_UMMA, 1) == L.OK
+    assert lib.gbfft_debug_set(L.DEBUG_TC_UMMA, request.param) == L.OK
     yield nr, L, lib
-    lib.gbfft_debug_set(L.DEBUG_TC_UMMA, 0)
+    lib.gbfft_debug_set(L.DEBUG_TC_UMMA, 1)
 
 
 @pytest.mark.parametrize("isign", [1, -1])
