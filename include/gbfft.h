@@ -118,6 +118,10 @@ long long gbfft_launch_count(int reset);
  *   GBFFT_DEBUG_TC_UMMA           1: the tensor-core batch form on tcgen05
  *                                 (the default), 0: on mma.sync (also
  *                                 GBFFT_TC_UMMA=0 at start-up)
+ *   GBFFT_DEBUG_CLUSTER_PASS      1: FP32 axes of 2^22..2^28 points run as
+ *                                 two passes on four-CTA clusters (also
+ *                                 GBFFT_CLUSTER_PASS=1 at start-up), 0: as
+ *                                 three per-CTA passes (the default, faster)
  * The batch settings drop the cached batch plan.  Nothing here hangs or
  * faults a GPU: every device wait stays bounded. */
 enum {
@@ -126,7 +130,8 @@ enum {
   GBFFT_DEBUG_BATCH_NEED_EXTRA = 3,
   GBFFT_DEBUG_BATCH_FIRST_RADIX_DELTA = 4,
   GBFFT_DEBUG_FUSED_TWIST = 5,
-  GBFFT_DEBUG_TC_UMMA = 6
+  GBFFT_DEBUG_TC_UMMA = 6,
+  GBFFT_DEBUG_CLUSTER_PASS = 7
 };
 int gbfft_debug_set(int key, long long value);
 int gbfft_profile(int enable);  /* also clears the records */

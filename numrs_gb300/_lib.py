@@ -72,6 +72,7 @@ DEBUG_BATCH_NEED_EXTRA = 3
 DEBUG_BATCH_FIRST_RADIX_DELTA = 4
 DEBUG_FUSED_TWIST = 5
 DEBUG_TC_UMMA = 6
+DEBUG_CLUSTER_PASS = 7
 
 _lib = None
 

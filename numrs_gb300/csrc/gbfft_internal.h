@@ -99,6 +99,9 @@ struct PassParams {
   int mirror_logU;
   int mirror_logV;
   double* aux;
+  // 1: the pass runs on a four-CTA cluster (k_pass_cl, FP32 two-pass plans):
+  // tiles of four columns, logC = 2, one cluster per tile
+  int cluster;
   // Per-slot parts of the global element indices of a tile, for layouts
   // without per-line pointer tables: slot k of thread tid holds tile element
   // e = tid + k*T, and its index is a per-thread base plus in_off[k] (load
@@ -157,6 +160,9 @@ cudaError_t launch_pass_df64(int sign, IOType in, IOType out, const PassParams& 
                              cudaStream_t st);
 cudaError_t launch_pass_tc32(int sign, IOType in, IOType out, const PassParams& p, int threads,
                              cudaStream_t st);
+// FP32 pass of a two-pass plan on a four-CTA cluster (fft_f32_cl_*.cu)
+cudaError_t launch_pass_cl_f32(int sign, IOType in, IOType out, const PassParams& p, int threads,
+                               cudaStream_t st);
 cudaError_t launch_twiddles(Form f, void* dense, void* partial, int dense_log, cudaStream_t st);
 
 // spectral / real-transform kernels (spectral.cu)

@@ -78,6 +78,11 @@ struct Ctx {
   // on the 20,000-transform batch
   bool tc_umma = true;
   bool fused_twist = true;  // realft twist on a pass (off: its own kernel)
+  // FP32 axes of 2^22..2^28 points in two cluster passes (k_pass_cl) instead
+  // of three per-CTA passes (GBFFT_CLUSTER_PASS=1 or the debug key).  Off by
+  // default: the exchange over distributed shared memory costs more than the
+  // HBM pass it saves (four1 2^28: 8.36 against 4.63 ms)
+  bool cluster_pass = false;
   // convlv/correl forward transforms: 0 = the two inputs as two n/2-point
   // realft lines, 1 = packed as one n-point complex FFT (twofft)
   int spectral_path = 0;
@@ -177,6 +182,8 @@ int init_locked(int device) {
   if (tc) g.tune_cache = tc;
   const char* um = getenv("GBFFT_TC_UMMA");
   g.tc_umma = !(um && um[0] == '0');
+  const char* cp = getenv("GBFFT_CLUSTER_PASS");
+  g.cluster_pass = cp && cp[0] == '1';
   g.inited = true;
   return GBFFT_OK;
 }
@@ -370,7 +377,8 @@ int launch_pass(Form f, int sign, IOType in, IOType out, const PassParams& p, in
   cudaError_t e;
   const double pts = (double)p.L * (double)p.nlines;
   ProfScope ps(PK_PASS, pts * (double)(io_bytes(in) + io_bytes(out)), 5.0 * pts * p.logR);
-  if (f == FORM_F64) e = launch_pass_f64(sign, in, out, p, threads, g.cur);
+  if (p.cluster) e = launch_pass_cl_f32(sign, in, out, p, threads, g.cur);
+  else if (f == FORM_F64) e = launch_pass_f64(sign, in, out, p, threads, g.cur);
   else if (f == FORM_F32) e = launch_pass_f32(sign, in, out, p, threads, g.cur);
   else if (f == FORM_TC32) e = launch_pass_tc32(sign, in, out, p, threads, g.cur);
   else e = launch_pass_df64(sign, in, out, p, threads, g.cur);
@@ -464,7 +472,7 @@ int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale = 1.
 bool twist_fits(const AxisPlan& ap, int twist) {
   if (ap.passes.empty()) return false;
   const PassParams& p = (twist > 0 ? ap.passes.back() : ap.passes.front()).p;
-  if (p.s != 1) return false;
+  if (p.s != 1 || p.cluster) return false;
   if (p.mode == 0) return p.logC >= 1 && (p.L >> p.logR) >= (1ll << p.logC);
   return ap.passes.size() == 1;
 }
@@ -567,8 +575,62 @@ int tune_tile(Form f, long long L, long long s, long long nlines, int lq_log, lo
   return best_tl;
 }
 
+// FP32 two-pass schedule of a long unit-stride axis: radices 2^ceil(logL/2)
+// and 2^floor(logL/2), each pass on four-CTA clusters of four columns
+// (k_pass_cl).  FP32 scratch between the passes mirrors the caller layout.
+constexpr int kClusterMinLog = 22;  // radix >= 2^11: at least 128 threads per CTA
+constexpr int kClusterTile = 99;    // plan-cache key of these plans
+bool cluster_fits(Form f, long long L, long long s, int lq_log) {
+  if (!g.cluster_pass || f != FORM_F32 || s != 1 || lq_log != 0) return false;
+  const int logL = ilog2((unsigned long long)L);
+  return logL >= kClusterMinLog && logL <= 2 * 14;
+}
+
+AxisPlan make_cluster_plan(long long L, long long nlines, long long lstride) {
+  AxisPlan ap;
+  const int logL = ilog2((unsigned long long)L);
+  const int radix[2] = {(logL + 1) / 2, logL / 2};
+  int logNs = 0;
+  for (int i = 0; i < 2; ++i) {
+    Pass ps;
+    PassParams& p = ps.p;
+    std::memset(&p, 0, sizeof p);
+    const int logR = radix[i];
+    p.L = L;
+    p.s = 1;
+    p.lstride = lstride;
+    p.nlines = nlines;
+    p.lq_log = 0;
+    p.logL = logL;
+    p.logR = logR;
+    p.logNs = logNs;
+    p.Ns = 1ll << logNs;
+    p.mode = 0;
+    p.logC = 2;
+    p.in_rcontig = 0;
+    p.out_rcontig = (logNs == 0) ? 1 : 0;
+    split_subpasses(logR - 2, p);  // the M = R/4-point DFTs of each CTA
+    p.tiles = nlines * ((L >> logR) >> 2);
+    p.scale = 1.0;
+    p.cluster = 1;
+    ps.threads = (1 << logR) / 16;
+    ps.in_user = (i == 0) ? 1 : 0;
+    ps.out_user = (i == 1) ? 1 : 0;
+    ap.passes.push_back(ps);
+    logNs += logR;
+  }
+  ap.scratch_elems = (size_t)((nlines - 1) * lstride + L);
+  return ap;
+}
+
 const AxisPlan& axis_plan(long long L, long long s, long long nlines, int lq_log,
                           long long lstride, Form f = FORM_F64) {
+  if (cluster_fits(f, L, s, lq_log)) {
+    auto key = std::make_tuple(L, s, nlines, lq_log, lstride, kClusterTile);
+    auto it = g_plans.find(key);
+    if (it != g_plans.end()) return it->second;
+    return g_plans.emplace(key, make_cluster_plan(L, nlines, lstride)).first->second;
+  }
   int tl = 12;
   if (g.autotune) {
     tune_load();
@@ -1362,6 +1424,9 @@ int gbfft_debug_set(int key, long long value) {
     case GBFFT_DEBUG_TC_UMMA:
       g.tc_umma = value != 0;
       batch_plan_free(g_batch);
+      return GBFFT_OK;
+    case GBFFT_DEBUG_CLUSTER_PASS:
+      g.cluster_pass = value != 0;
       return GBFFT_OK;
     case GBFFT_DEBUG_BATCH_FIRST_RADIX_DELTA:
       if (value < -12 || value > 12) return fail(GBFFT_INVALID_ARG, "debug_set: value out of range");
