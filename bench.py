@@ -76,12 +76,14 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large",
                     choices=["large", "convlv", "four1", "batch", "fourn", "rlft3", "c1", "convbatch",
-                             "peaks"])
+                             "peaks", "sharded"])
     ap.add_argument("--form", default="fp64", choices=["fp64", "df64", "fp32", "tc32"])
     ap.add_argument("--no-forms", action="store_true", help="skip the extra precision forms")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched target in the default line")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--log2n", type=int, default=0, help="four1 workload size (default 2^24; large: 2^28)")
+    ap.add_argument("--shares", type=int, default=0,
+                    help="sharded workload in one process: P shares on this GPU (exchanges as copies)")
     return ap.parse_args()
 
 
@@ -1061,13 +1063,59 @@ def run_c1(args, world, rank, local):
     torch.cuda.synchronize()
     steps = max(args.steps, 100)
     total_ms, launches, clk = _timed(args, local, step, None, steps)
+    # the same round trip captured once in a CUDA graph and replayed: the
+    # device-side latency without the per-call host work (the library
+    # launches on the caller's current stream)
+    graph = {"us_per_roundtrip": None}
+    try:
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            step()
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        with torch.cuda.graph(g):
+            step()
+        for _ in range(10):
+            g.replay()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        reps = 1000
+        e0.record()
+        for _ in range(reps):
+            g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        graph["us_per_roundtrip"] = 1e3 * e0.elapsed_time(e1) / reps
+    except Exception as ex:  # capture refused: report why
+        graph["note"] = str(ex).splitlines()[0][:200]
     nr.set_async(False)
     if rank != 0:
         return None
+    # CPU baseline: the oracle's round trip on one core, about a second of work
+    import oracle as O
+    xs = x.copy()
+    n_rt = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < 1.0:
+        O.four1(xs, 4096, 1)
+        O.four1(xs, 4096, -1)
+        xs *= 1.0 / 4096
+        n_rt += 1
+    cpu_s = (time.perf_counter() - t0) / n_rt
+    flops = 2 * 5.0 * 4096 * 12
     return _simple_line(args, world, "four1 N=4096 round trip (+1, -1, x1/N), one transform",
-                        2 * 5.0 * 4096 * 12, total_ms, steps, launches, clk,
+                        flops, total_ms, steps, launches, clk,
                         {"us_per_roundtrip": 1e3 * total_ms / steps,
-                         "accuracy": {"roundtrip_rel_l2": err}})
+                         "graph_replay": graph,
+                         "accuracy": {"roundtrip_rel_l2": err},
+                         "cpu_baseline": {"value": flops / cpu_s / 1e9, "unit": "GFLOP/s",
+                                          "us_per_roundtrip": cpu_s * 1e6, "cores": 1,
+                                          "kind": "port",
+                                          "sample": "%d oracle round trips of 4096 points on one "
+                                                    "host thread" % n_rt}})
 
 
 def run_peaks(args, world, rank, local):
@@ -1111,6 +1159,66 @@ def run_peaks(args, world, rank, local):
             "config": {"workload": "torch.matmul square GEMMs: f64 4096^3 and f32 8192^3, TF32 off"},
             "gemm": res, "used_in_bench": {"fp64_peak_tflops": FP64_PEAK_TFLOPS,
                                             "fp32_peak_tflops": FP32_PEAK_TFLOPS}}
+
+
+def run_sharded(args, world, rank, local):
+    """four1 of 2^log2n points (default 2^28, FP64) split over the ranks with
+    the four-step schedule of numrs_gb300.dist: local column transforms, the
+    twiddle kernel, one all-to-all, local row transforms, natural-order block
+    input and output (two more all-to-alls).  Total work is fixed (strong
+    scaling).  With --shares P in one process, the P shares live on this GPU
+    and the exchanges are device copies: the whole transform's local work and
+    data movement on one GPU."""
+    import torch
+    import numrs_gb300 as nr
+    from numrs_gb300 import dist as D
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    log2n = args.log2n or LARGE_LOG2N
+    N = 1 << log2n
+    emulate = args.shares > 0
+    P = args.shares if emulate else world
+    x = large_input(log2n)
+    parts = D.to_layout(x, N, P, "block")
+    if emulate:
+        src = [torch.from_numpy(p).to(dev) for p in parts]
+        run = lambda: D.four1_sharded_local(src, N, 1, "block", "block", form=args.form)
+    else:
+        src = torch.from_numpy(parts[rank]).to(dev)
+        run = lambda: D.four1_sharded(src, N, 1, "block", "block", form=args.form)
+    del parts
+    nr.set_async(True)
+    out = run()
+    torch.cuda.synchronize()
+    # accuracy of this rank's (or the shares') output against the single-GPU transform
+    ref = torch.from_numpy(x).to(dev)
+    nr.four1(ref, N, 1, form=args.form)
+    got = torch.cat(out) if emulate else out
+    lo = 0 if emulate else rank * (2 * N // P)
+    want = ref[lo:lo + got.numel()]
+    err = float(torch.linalg.vector_norm(got - want) / torch.linalg.vector_norm(want))
+    del ref, got, want, out
+    torch.cuda.empty_cache()
+    for _ in range(max(args.warmup, 3)):
+        run()
+    torch.cuda.synchronize()
+    barrier(world)
+    total_ms, launches, clk = _timed(args, local, run, None, args.steps)
+    total_ms = max_over_ranks(total_ms, world)
+    nr.set_async(False)
+    if rank != 0:
+        return None
+    flops = 5.0 * N * log2n
+    line = _simple_line(args, world, "four1 complex FFT, nn=2^%d split over %d %s with the four-step "
+                        "schedule (one transform per step)" % (log2n, P, "shares on one GPU" if emulate else "ranks"),
+                        flops, total_ms, args.steps, launches, clk,
+                        {"accuracy": {"rel_l2_vs_single_gpu_four1": err}})
+    # one transform per step whatever the rank count: total work is fixed
+    line["value"] = flops * args.steps / (total_ms / 1e3) / 1e9
+    line["scaling"] = "strong"
+    line["config"]["shares"] = P
+    line["config"]["exchange"] = "device copies (one process)" if emulate else "torch.distributed all_to_all_single"
+    return line
 
 
 def run_convbatch(args, world, rank, local):
@@ -1185,7 +1293,7 @@ def main():
         dist.init_process_group("nccl")
     fn = {"large": run_large, "four1": run_four1, "batch": run_batch, "fourn": run_nd,
           "rlft3": run_nd, "c1": run_c1, "convbatch": run_convbatch,
-          "peaks": run_peaks}.get(args.workload)
+          "peaks": run_peaks, "sharded": run_sharded}.get(args.workload)
     if fn is None:
         run_convlv(args, world, rank, local)
     else:

@@ -268,6 +268,16 @@ int gbfft_correl_batch(const double* const* data1, const size_t* n1, const doubl
 int gbfft_correl_normalized(const double* data1, size_t n1, const double* data2, size_t n2,
                             double* ans, int fast, const gbfft_opts* opts);
 
+/* Four-step twiddle of a four1 of n points split across ranks (one GPU each;
+ * the Python mirror's numrs_gb300.dist runs column transforms, this twiddle,
+ * one all-to-all and row transforms).  data: `lines` lines of `len` complex
+ * values in DEVICE memory (opts->device_ptrs set); element k of line c is
+ * multiplied by exp(isign 2 pi i ((line0 + c) k mod n) / n).  n and len are
+ * powers of two, len <= n <= 2^28.  No crate counterpart: the crate's four1
+ * (src/FFT_1.rs:5-107) runs on one host. */
+int gbfft_twiddle_lines(double* data, size_t lines, size_t len, size_t line0, size_t n, int isign,
+                        const gbfft_opts* opts);
+
 /* magnitude_spectrum / power_spectrum: src/FFT_1.rs:206,218.  c holds nn
  * interleaved complex values; out[nn].  The crate maps chunks(2) of its slice,
  * so for an odd-length slice it appends one 0.0 for the trailing half chunk:

@@ -35,7 +35,7 @@ __all__ = [
     "autocorrel", "magnitude_spectrum", "power_spectrum", "real_to_complex",
     "complex_to_real", "ConvlvError", "CorrelError", "GbfftError", "launch_count",
     "FFTBatch", "four1_many", "set_async", "profile", "profile_read", "four1_noalloc",
-    "four1_spectrum", "set_spectral_path", "fourfs",
+    "four1_spectrum", "set_spectral_path", "fourfs", "twiddle_lines",
     "correl_normalized", "correl_normalized_fast", "autocorrel_fast", "ConvlvProcessor",
     "RealFTProcessor", "TwoFFTProcessor",
 ]
@@ -215,6 +215,20 @@ def four1_many(data, nn, count, isign, dist=None, form="fp64"):
     dist = 2 * nn if dist is None else dist
     o = _opts([a], form)
     _check(_lib.load().gbfft_four1_many(a.ptr, nn, count, dist, isign, ctypes.byref(o)))
+
+
+def twiddle_lines(data, lines, length, line0, n, isign):
+    """Four-step twiddle of a transform of n points split across ranks (see
+    ``numrs_gb300.dist``): element k of line c of ``data`` (a CUDA float64
+    tensor of ``lines`` lines of ``length`` complex values) times
+    exp(isign 2 pi i ((line0 + c) k mod n) / n)."""
+    a = _Arg(data, True)
+    if not a.dev:
+        raise ValueError("twiddle_lines takes a CUDA tensor")
+    if a.size < 2 * lines * length:
+        raise ValueError("data holds %d doubles, need %d" % (a.size, 2 * lines * length))
+    o = _opts([a], "fp64")
+    _check(_lib.load().gbfft_twiddle_lines(a.ptr, lines, length, line0, n, isign, ctypes.byref(o)))
 
 
 class FFTProcessor:

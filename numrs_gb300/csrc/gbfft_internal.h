@@ -235,6 +235,8 @@ cudaError_t launch_moment(const double* x, long long n, double shift, int p, dou
                           double* out, cudaStream_t st);
 cudaError_t launch_standardize(const double* x, long long n, double mean, double stdv,
                                double* out, cudaStream_t st);
+cudaError_t launch_twiddle_lines(double* data, long long lines, int loglen, long long line0,
+                                 int logn, int isign, const Twiddles& tw, cudaStream_t st);
 cudaError_t launch_spectrum(int kind, const double* c, double* out, long long nn,
                             cudaStream_t st);
 

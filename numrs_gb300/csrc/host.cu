@@ -692,12 +692,25 @@ int check_form(const Call& c) {
 // Stream handling: a device-pointer call runs on the caller's stream (NULL is
 // the default stream, so the call is ordered after earlier default-stream
 // work); host-pointer calls run on the library stream.
+// Calls on a stream that is capturing a CUDA graph neither wait on nor record
+// the ordering event: an event recorded outside a capture cannot be waited on
+// inside it, and the graph itself orders what it captures.
 struct StreamScope {
+  bool capturing = false;
   explicit StreamScope(const Call& c) {
     g.cur = c.dev() ? (cudaStream_t)c.o->stream : g.stream;
-    if (g.order_pending && g.order_stream != g.cur) cudaStreamWaitEvent(g.cur, g.order_ev, 0);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (c.dev() && cudaStreamIsCapturing(g.cur, &cs) == cudaSuccess)
+      capturing = cs != cudaStreamCaptureStatusNone;
+    if (!capturing && g.order_pending && g.order_stream != g.cur)
+      cudaStreamWaitEvent(g.cur, g.order_ev, 0);
   }
   int finish(const Call& c) {
+    if (capturing) {
+      CK(cudaGetLastError());
+      g.cur = g.stream;
+      return GBFFT_OK;
+    }
     if (!c.dev() || !c.o->async) {
       CK(cudaStreamSynchronize(g.cur));
       g.order_pending = false;
@@ -2246,6 +2259,29 @@ static int spectrum_call(int kind, const double* cdata, size_t nn, double* out,
   CK(launch_spectrum(kind, in, o, (long long)nn, g.cur));
   g.launches++;
   if (!c.dev()) TRY(d2h(out, o, nn * sizeof(double)));
+  return ss.finish(c);
+}
+
+int gbfft_twiddle_lines(double* data, size_t lines, size_t len, size_t line0, size_t n, int isign,
+                        const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  if (!data) return fail(GBFFT_INVALID_ARG, "twiddle_lines: null data");
+  if (!c.dev()) return fail(GBFFT_INVALID_ARG, "twiddle_lines: device data only");
+  TRY(dev_aligned(c, "twiddle_lines", {data}));
+  if (isign != 1 && isign != -1) return fail(GBFFT_INVALID_ARG, "twiddle_lines: isign must be +-1");
+  if (!is_pow2(n) || !is_pow2(len) || len > n || ilog2(n) > kMaxLog)
+    return fail(GBFFT_UNSUPPORTED_SIZE,
+                "twiddle_lines: n=%zu and len=%zu must be powers of two, len <= n <= 2^%d", n, len,
+                kMaxLog);
+  if (lines == 0 || n == 1) return GBFFT_OK;
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  Twiddles tw;
+  TRY(tables(FORM_F64, tw));
+  CK(launch_twiddle_lines(data, (long long)lines, ilog2(len), (long long)line0, ilog2(n), isign,
+                          tw, g.cur));
+  g.launches++;
   return ss.finish(c);
 }
 

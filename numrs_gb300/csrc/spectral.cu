@@ -713,6 +713,37 @@ cudaError_t launch_scale(double* data, long long count, double s, cudaStream_t s
   return cudaGetLastError();
 }
 
+// Four-step twiddle of a transform of n = 2^logn points sharded over ranks:
+// element k of line c, data[c len + k], times w_n^((line0 + c) k) with
+// w_n = exp(isign 2 pi i / n).  The exponent is reduced mod n in 64-bit
+// integers and looked up in the FP64 twiddle tables.
+__global__ void k_twiddle_lines(double* data, long long lines, int loglen, long long line0,
+                                int logn, int isign, Twiddles tw) {
+  const long long total = lines << loglen;
+  const unsigned long long mask = (1ull << logn) - 1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long c = (unsigned long long)(i >> loglen);
+    const unsigned long long k = (unsigned long long)(i & ((1ll << loglen) - 1));
+    const unsigned long long e = ((unsigned long long)line0 + c) * k & mask;
+    if (e == 0) continue;
+    d2* q = reinterpret_cast<d2*>(data) + i;
+    const d2 v = *q;
+    const F64::C w = twiddle<F64>(tw, logn, (unsigned)e, isign);
+    *q = d2{v.x * w.x - v.y * w.y, v.x * w.y + v.y * w.x};
+  }
+}
+
+cudaError_t launch_twiddle_lines(double* data, long long lines, int loglen, long long line0,
+                                 int logn, int isign, const Twiddles& tw, cudaStream_t st) {
+  const long long total = lines << loglen;
+  long long blocks = (total + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  k_twiddle_lines<<<(int)blocks, 256, 0, st>>>(data, lines, loglen, line0, logn, isign, tw);
+  return cudaGetLastError();
+}
+
 // magnitude_spectrum / power_spectrum (src/FFT_1.rs:206-228)
 __global__ void k_spectrum(int kind, const double* c, double* out, long long nn) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nn;
