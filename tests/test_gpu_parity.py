@@ -218,6 +218,22 @@ def test_twofft(nr, n):
     assert f1[2 * n] == 7.0 and f2[2 * n + 1] == 7.0  # tail left untouched
 
 
+@pytest.mark.parametrize("form", ["fp32", "tc32", "df64"])
+@pytest.mark.parametrize("n", [4, 256, 4096, 1 << 16, 1 << 20])
+def test_twofft_forms(nr, form, n):
+    """twofft (src/FFT_2.rs:3) in the other forms: both spectra against the
+    oracle's at the form's bar."""
+    a, b = W.normal(5, n), W.normal(6, n)
+    f1 = np.zeros(2 * n + 2)
+    f2 = np.zeros(2 * n + 2)
+    nr.twofft(a, b, f1, f2, form=form)
+    r1, r2 = O.twofft(a, b)
+    bar = 1e-12 if form == "df64" else 1e-6
+    for got, ref, what in ((f1, r1, "fft1"), (f2, r2, "fft2")):
+        e = rel_l2(got[:2 * n], ref[:2 * n])
+        assert e <= bar, "twofft %s %s n=%d rel-L2 %.3e" % (form, what, n, e)
+
+
 @pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("shape", [(8, 16, 32), (4, 4), (2, 8192), (8192, 4), (64, 2, 128), (16, 16, 16, 16)])
 def test_fourn(nr, form, shape):
@@ -363,6 +379,33 @@ def _exact_trig(kind, y, n, isign=1):
     if kind == "cosft1":
         return sf.dct(y, type=1) / 2
     return sf.dct(y, type=2 if isign == 1 else 3) / 2
+
+
+@pytest.mark.parametrize("form", ["fp32", "tc32"])
+@pytest.mark.parametrize("n", [4, 64, 1024, 4096, 1 << 16, 1 << 20])
+def test_sine_cosine_transforms_fp32_forms(nr, form, n):
+    """sinft, cosft1 and cosft2 (both directions) in the FP32-pipe forms
+    against the exact transforms (scipy).  The algorithm (src/Cos_FT.rs:7-68,
+    src/Cos_FT2.rs:7-173, and the sine transform) turns realft outputs into
+    running sums over n/2 terms, which grow each output's rounding error like
+    sqrt(n): the FP64 path shows the same growth relative to its unit
+    roundoff (1.7e-13, about 1500 units, at 2^20).  The bar is that growth
+    in FP32 units, 4 * 2^-24 * sqrt(n) (at least the FFT bar 1e-6)."""
+    bar = max(1e-6, 4 * 2.0 ** -24 * np.sqrt(n))
+    cases = [("sinft", W.normal(n + 5, n), None), ("cosft1", W.normal(n + 6, n + 1), None),
+             ("cosft2", W.normal(n + 7, n), 1), ("cosft2", W.normal(n + 7, n), -1)]
+    for kind, y, isign in cases:
+        d = y.copy()
+        y0 = y.copy()
+        if kind == "sinft":
+            nr.sinft(d, n, form=form)
+            y0[0] = 0.0
+        elif kind == "cosft1":
+            nr.cosft1(d, n, form=form)
+        else:
+            nr.cosft2(d, n, isign, form=form)
+        e = rel_l2(d, _exact_trig(kind, y0, n, isign or 1))
+        assert e <= bar, "%s %s n=%d isign=%s rel-L2 %.3e (bar %.1e)" % (form, kind, n, isign, e, bar)
 
 
 @pytest.mark.parametrize("form", ["fp64", "df64"])
