@@ -161,11 +161,11 @@ __device__ __forceinline__ void dftq(typename F::C* v) {
 // One in-CTA Stockham sub-pass of radix Q over C columns of R points held in
 // shared memory (column c at c*R, padded).  Every thread owns 16/Q butterflies.
 // ---------------------------------------------------------------------------
-template <class F, int SG, int Q>
+template <class F, int SG, int Q, int EPT = kEPT>
 __device__ __forceinline__ void subpass(typename F::S* sm, int logR, int cs, int logNs,
                                         const Twiddles& tw, int tid, int T) {
   using C = typename F::C;
-  constexpr int B = kEPT / Q;
+  constexpr int B = EPT / Q;
   constexpr int LQ = (Q == 2) ? 1 : (Q == 4) ? 2 : (Q == 8) ? 3 : 4;
   constexpr int sh = F::kPadShift;
   const int logRQ = logR - LQ;
@@ -351,8 +351,9 @@ __device__ __forceinline__ long long thread_base_out(const PassParams& p, long l
 
 // The R-point DFTs of the tile's columns in shared memory: the pass's
 // sub-passes in order.  Starts after a barrier that made the tile visible and
-// ends with one.
-template <class F, int SG, int T>
+// ends with one.  EPT elements per thread allow sub-passes of radix <= EPT
+// (the planner splits accordingly).
+template <class F, int SG, int T, int EPT = kEPT>
 __device__ __forceinline__ void run_subpasses(const PassParams& p, typename F::S* sm, int cs,
                                               int tid) {
   const int logR = p.logR;
@@ -361,17 +362,21 @@ __device__ __forceinline__ void run_subpasses(const PassParams& p, typename F::S
     const int lq = p.q[k];
     switch (lq) {
       case 4:
-        if constexpr (F::kTensor) {
-          Dft16Frags A;
-          dft16_frags<SG>(reinterpret_cast<const f2*>(p.tw.dense), A);
-          subpass16_tc<SG>(reinterpret_cast<f2*>(sm), logR, cs, logNsub, p.tw, A, tid);
-        } else {
-          subpass<F, SG, 16>(sm, logR, cs, logNsub, p.tw, tid, T);
+        if constexpr (EPT >= 16) {
+          if constexpr (F::kTensor) {
+            Dft16Frags A;
+            dft16_frags<SG>(reinterpret_cast<const f2*>(p.tw.dense), A);
+            subpass16_tc<SG>(reinterpret_cast<f2*>(sm), logR, cs, logNsub, p.tw, A, tid);
+          } else {
+            subpass<F, SG, 16, EPT>(sm, logR, cs, logNsub, p.tw, tid, T);
+          }
         }
         break;
-      case 3: subpass<F, SG, 8>(sm, logR, cs, logNsub, p.tw, tid, T); break;
-      case 2: subpass<F, SG, 4>(sm, logR, cs, logNsub, p.tw, tid, T); break;
-      default: subpass<F, SG, 2>(sm, logR, cs, logNsub, p.tw, tid, T); break;
+      case 3:
+        if constexpr (EPT >= 8) subpass<F, SG, 8, EPT>(sm, logR, cs, logNsub, p.tw, tid, T);
+        break;
+      case 2: subpass<F, SG, 4, EPT>(sm, logR, cs, logNsub, p.tw, tid, T); break;
+      default: subpass<F, SG, 2, EPT>(sm, logR, cs, logNsub, p.tw, tid, T); break;
     }
     logNsub += lq;
   }
@@ -379,7 +384,7 @@ __device__ __forceinline__ void run_subpasses(const PassParams& p, typename F::S
 
 // The store of a transformed tile at the autosorted positions (after the
 // barrier that ends the last sub-pass).
-template <class F, int SG, int OUT, int T>
+template <class F, int SG, int OUT, int T, int EPT = kEPT>
 __device__ __forceinline__ void store_tile(const PassParams& p, long long line0, long long j0,
                                            const typename F::S* sm, int tid) {
   using C = typename F::C;
@@ -394,7 +399,7 @@ __device__ __forceinline__ void store_tile(const PassParams& p, long long line0,
     OE* dst = reinterpret_cast<OE*>(p.out) + tb;
     const long long rem = (p.mode == 0) ? (1ll << 62) : p.nlines - line0;
 #pragma unroll 4
-    for (int k = 0; k < kEPT; ++k) {
+    for (int k = 0; k < EPT; ++k) {
       const int e = tid + k * T;
       int c, r;
       elem_cr(e, p.out_rcontig, logR, logC, c, r);
@@ -409,7 +414,7 @@ __device__ __forceinline__ void store_tile(const PassParams& p, long long line0,
     return;
   }
 #pragma unroll 4
-  for (int k = 0; k < kEPT; ++k) {
+  for (int k = 0; k < EPT; ++k) {
     const int e = tid + k * T;
     int c, r;
     elem_cr(e, p.out_rcontig, logR, logC, c, r);
@@ -426,11 +431,11 @@ __device__ __forceinline__ void store_tile(const PassParams& p, long long line0,
 
 // The R-point DFTs of the tile's columns, then the store at the autosorted
 // positions.  Starts after a barrier that made the staged tile visible.
-template <class F, int SG, int OUT, int T>
+template <class F, int SG, int OUT, int T, int EPT = kEPT>
 __device__ __forceinline__ void tile_compute_store(const PassParams& p, long long line0,
                                                    long long j0, typename F::S* sm, int tid) {
-  run_subpasses<F, SG, T>(p, sm, col_stride(p.logR, F::kPadShift), tid);
-  store_tile<F, SG, OUT, T>(p, line0, j0, sm, tid);
+  run_subpasses<F, SG, T, EPT>(p, sm, col_stride(p.logR, F::kPadShift), tid);
+  store_tile<F, SG, OUT, T, EPT>(p, line0, j0, sm, tid);
 }
 
 // Address of tile element e in global memory, input side, for tiles whose
@@ -468,16 +473,16 @@ __device__ __forceinline__ void load_elem(const IE* src, IE& dst) {
 // The sixteen raw elements of thread tid's slots (zero outside the lines).
 // All loads are issued before any is used, so that each SM keeps enough
 // bytes in flight to cover the memory latency.
-template <class IE, int IN, int T, bool L2_ONLY>
+template <class IE, int IN, int T, bool L2_ONLY, int EPT = kEPT>
 __device__ __forceinline__ void load_tile_raw(const PassParams& p, long long line0, long long j0,
-                                              int tid, IE (&raw)[kEPT]) {
+                                              int tid, IE (&raw)[EPT]) {
   if (p.in_ptrs == nullptr) {
     // linear layout: per-thread base plus the slot offsets in_off[k]
     long long ct;
     const IE* src = reinterpret_cast<const IE*>(p.in) + thread_base_in(p, line0, j0, tid, ct);
     const long long rem = (p.mode == 0) ? (1ll << 62) : p.nlines - line0;
 #pragma unroll
-    for (int k = 0; k < kEPT; ++k) {
+    for (int k = 0; k < EPT; ++k) {
       long long ck, rk;
       tile_cr((long long)k * T, p.in_rcontig, p.logR, p.logC, ck, rk);
       if (ct + ck < rem) load_elem<IE, L2_ONLY>(src + p.in_off[k], raw[k]);
@@ -485,7 +490,7 @@ __device__ __forceinline__ void load_tile_raw(const PassParams& p, long long lin
     }
   } else {
 #pragma unroll
-    for (int k = 0; k < kEPT; ++k) {
+    for (int k = 0; k < EPT; ++k) {
       bool valid;
       const IE* src = elem_src<IN>(p, line0, j0, tid + k * T, valid);
       if (valid) load_elem<IE, L2_ONLY>(src, raw[k]);
@@ -496,18 +501,18 @@ __device__ __forceinline__ void load_tile_raw(const PassParams& p, long long lin
 
 // One full tile from global memory.  L2_ONLY loads bypass L1 (data written by
 // other CTAs of the same launch).
-template <class F, int SG, int IN, int OUT, int T, bool L2_ONLY>
+template <class F, int SG, int IN, int OUT, int T, bool L2_ONLY, int EPT = kEPT>
 __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
                                           typename F::S* sm, int tid) {
   using IE = typename IOElem<IN>::T;
   long long line0, j0;
   tile_origin(p, tile, line0, j0);
-  IE raw[kEPT];
-  load_tile_raw<IE, IN, T, L2_ONLY>(p, line0, j0, tid, raw);
+  IE raw[EPT];
+  load_tile_raw<IE, IN, T, L2_ONLY, EPT>(p, line0, j0, tid, raw);
 #pragma unroll
-  for (int k = 0; k < kEPT; ++k) stage_elem<F, SG, IN>(p, line0, j0, tid + k * T, raw[k], sm);
+  for (int k = 0; k < EPT; ++k) stage_elem<F, SG, IN>(p, line0, j0, tid + k * T, raw[k], sm);
   __syncthreads();
-  tile_compute_store<F, SG, OUT, T>(p, line0, j0, sm, tid);
+  tile_compute_store<F, SG, OUT, T, EPT>(p, line0, j0, sm, tid);
 }
 
 // ---------------------------------------------------------------------------
@@ -1028,6 +1033,50 @@ cudaError_t launch_pass_t(const PassParams& p, int threads, cudaStream_t st) {
     case 64: return launch_pass_one<F, SG, IN, OUT, 64>(p, st);
     default: return launch_pass_one<F, SG, IN, OUT, 32>(p, st);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Latency kernel for the latency-mode plans (lone transforms of 2^10..2^12
+// points, two passes).  GB300 issues FP64 at 2 lanes per SM, so the FP64 time
+// of a pass is set by how many SMs share its arithmetic: 16-point-per-thread
+// tiles of 512 points put a 4096-point pass on 8 one-warp CTAs (8 SMs).
+// These tiles hold 128 points, four per thread of one warp, with radix-2/4
+// sub-passes, so the same pass runs on 32 SMs.  Staged tiles for every form;
+// the radix <= 4 sub-passes run on the CUDA cores in the tensor-core form too.
+// ---------------------------------------------------------------------------
+constexpr int kLatThreads = 32;
+
+template <class F, int SG, int IN, int OUT>
+__global__ void __launch_bounds__(kLatThreads) k_pass_lat(PassParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  pass_tile<F, SG, IN, OUT, kLatThreads, false, kLatencyEPT>(
+      p, blockIdx.x, reinterpret_cast<typename F::S*>(smem_raw), threadIdx.x);
+}
+
+template <class F, int SG, int IN, int OUT>
+inline cudaError_t launch_lat_one(const PassParams& p, cudaStream_t st) {
+  constexpr int E = kLatencyEPT * kLatThreads;
+  const size_t smem = sizeof(typename F::S) * (size_t)(E + (E >> F::kPadShift) + E / 16);
+  if (p.tiles <= 0 || p.tiles > 0x7FFFFFFFll) return cudaErrorInvalidValue;
+  if ((1 << (p.logR + p.logC)) != E || p.logR < 4) return cudaErrorInvalidValue;
+  for (int k = 0; k < p.nq; ++k)
+    if (p.q[k] < 1 || p.q[k] > 2) return cudaErrorInvalidValue;
+  PassParams q = p;
+  set_slot_offsets(q, kLatThreads);
+  k_pass_lat<F, SG, IN, OUT><<<dim3((unsigned)q.tiles), kLatThreads, smem, st>>>(q);
+  return cudaGetLastError();
+}
+
+template <class F, int SG>
+cudaError_t dispatch_lat(IOType in, IOType out, const PassParams& p, cudaStream_t st) {
+  constexpr int S = (F::kind == 2) ? IO_F4 : IO_F2;
+  if (in == IO_D2 && out == IO_D2) return launch_lat_one<F, SG, IO_D2, IO_D2>(p, st);
+  if constexpr (F::kind != 0) {
+    if (in == IO_D2 && out == S) return launch_lat_one<F, SG, IO_D2, S>(p, st);
+    if (in == S && out == IO_D2) return launch_lat_one<F, SG, S, IO_D2>(p, st);
+    if (in == S && out == S) return launch_lat_one<F, SG, S, S>(p, st);
+  }
+  return cudaErrorInvalidValue;
 }
 
 // All IO combinations of one form and direction (FP64 uses double I/O only).

@@ -38,6 +38,7 @@ __host__ __device__ constexpr size_t partial_entries(int dense_log) {
 }
 
 constexpr int kTileEPT = 16;  // complex elements per thread per tile
+constexpr int kLatencyEPT = 4;  // elements per thread in the latency kernel's tiles
 
 struct Twiddles {
   const void* dense = nullptr;
@@ -102,6 +103,9 @@ struct PassParams {
   // 1: the pass runs on a four-CTA cluster (k_pass_cl, FP32 two-pass plans):
   // tiles of four columns, logC = 2, one cluster per tile
   int cluster;
+  // 1: a latency-mode pass (k_pass_lat): one-warp tiles of 128 points, four
+  // per thread, radix-2/4 sub-passes
+  int lat;
   // Per-slot parts of the global element indices of a tile, for layouts
   // without per-line pointer tables: slot k of thread tid holds tile element
   // e = tid + k*T, and its index is a per-thread base plus in_off[k] (load
@@ -160,6 +164,9 @@ cudaError_t launch_pass_df64(int sign, IOType in, IOType out, const PassParams& 
                              cudaStream_t st);
 cudaError_t launch_pass_tc32(int sign, IOType in, IOType out, const PassParams& p, int threads,
                              cudaStream_t st);
+// latency-mode pass of any form (fft_lat.cu)
+cudaError_t launch_pass_lat(Form f, int sign, IOType in, IOType out, const PassParams& p,
+                            cudaStream_t st);
 // FP32 pass of a two-pass plan on a four-CTA cluster (fft_f32_cl_*.cu)
 cudaError_t launch_pass_cl_f32(int sign, IOType in, IOType out, const PassParams& p, int threads,
                                cudaStream_t st);

@@ -269,6 +269,13 @@ struct AxisPlan {
   size_t scratch_elems = 0;
 };
 
+// Sub-passes of radix <= 4 (latency tiles hold four points per thread).
+void split_subpasses_r4(int logR, PassParams& p) {
+  p.nq = (logR + 1) / 2;
+  for (int i = 0; i < 4; ++i) p.q[i] = 0;
+  for (int i = 0; i < p.nq; ++i) p.q[i] = (i < logR / 2) ? 2 : 1;
+}
+
 void split_subpasses(int logR, PassParams& p) {
   int nsub = (logR + 3) / 4;
   if (nsub < 1) nsub = 1;
@@ -280,10 +287,11 @@ void split_subpasses(int logR, PassParams& p) {
 
 // Latency mode: one or two small transforms (at most 8192 points in all) would
 // run on one or two SMs in a single pass, and an FP64 transform of 4096 points
-// then takes ~40 us on one SM.  Two passes of 512-point tiles spread the same
-// work over 8-16 SMs.
+// then takes ~40 us on one SM (GB300 issues FP64 at 2 lanes per SM).  Two
+// passes of 128-point one-warp tiles (k_pass_lat, four points per thread)
+// spread the same work over 32-64 SMs.
 constexpr long long kLatencyMaxWork = 8192;
-constexpr int kLatencyTileLog = 9;
+constexpr int kLatencyTileLog = 7;  // kLatencyEPT points x 32 threads
 
 // tileLog: log2 of the complex elements per CTA tile (10..12); multi-pass
 // radices are kept 4 columns below it so that strided rows stay >= 64 bytes.
@@ -344,11 +352,15 @@ AxisPlan make_axis_plan(long long L, long long s, long long nlines, int lq_log,
       p.in_rcontig = (s == 1) ? 1 : 0;
       p.out_rcontig = (s == 1) ? 1 : 0;
     }
-    // at least one full warp: 16 * 32 = 512 elements per tile
-    if (logR + logC < 9) logC = 9 - logR;
+    // at least one full warp: 16 * 32 = 512 elements per tile (latency tiles:
+    // 4 * 32 = 128)
+    const int minTile = latency ? kLatencyTileLog : 9;
+    if (logR + logC < minTile) logC = minTile - logR;
     p.logC = logC;
-    ps.threads = (1 << (logR + logC)) / 16;
-    split_subpasses(logR, p);
+    ps.threads = (1 << (logR + logC)) / (latency ? kLatencyEPT : kTileEPT);
+    if (latency) split_subpasses_r4(logR, p);
+    else split_subpasses(logR, p);
+    p.lat = latency ? 1 : 0;
     if (p.mode == 0) p.tiles = nlines * (LR >> logC);
     else p.tiles = LR * ((nlines + (1ll << logC) - 1) >> logC);
     p.do_scale = 0;
@@ -378,6 +390,7 @@ int launch_pass(Form f, int sign, IOType in, IOType out, const PassParams& p, in
   const double pts = (double)p.L * (double)p.nlines;
   ProfScope ps(PK_PASS, pts * (double)(io_bytes(in) + io_bytes(out)), 5.0 * pts * p.logR);
   if (p.cluster) e = launch_pass_cl_f32(sign, in, out, p, threads, g.cur);
+  else if (p.lat) e = launch_pass_lat(f, sign, in, out, p, g.cur);
   else if (f == FORM_F64) e = launch_pass_f64(sign, in, out, p, threads, g.cur);
   else if (f == FORM_F32) e = launch_pass_f32(sign, in, out, p, threads, g.cur);
   else if (f == FORM_TC32) e = launch_pass_tc32(sign, in, out, p, threads, g.cur);
@@ -472,7 +485,7 @@ int run_axis(Form f, int sign, const AxisPlan& ap, void* data, double scale = 1.
 bool twist_fits(const AxisPlan& ap, int twist) {
   if (ap.passes.empty()) return false;
   const PassParams& p = (twist > 0 ? ap.passes.back() : ap.passes.front()).p;
-  if (p.s != 1 || p.cluster) return false;
+  if (p.s != 1 || p.cluster || p.lat) return false;
   if (p.mode == 0) return p.logC >= 1 && (p.L >> p.logR) >= (1ll << p.logC);
   return ap.passes.size() == 1;
 }
