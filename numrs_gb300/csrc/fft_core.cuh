@@ -1036,8 +1036,8 @@ cudaError_t launch_pass_t(const PassParams& p, int threads, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
-// Latency kernel for the latency-mode plans (lone transforms of 2^10..2^12
-// points, two passes).  GB300 issues FP64 at 2 lanes per SM, so the FP64 time
+// Latency kernel for the latency-mode plans (lone transforms of 2^10..2^14
+// points, two passes of radix <= 2^7).  GB300 issues FP64 at 2 lanes per SM, so the FP64 time
 // of a pass is set by how many SMs share its arithmetic: 16-point-per-thread
 // tiles of 512 points put a 4096-point pass on 8 one-warp CTAs (8 SMs).
 // These tiles hold 128 points, four per thread of one warp, with radix-2/4

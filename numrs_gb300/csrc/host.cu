@@ -285,12 +285,13 @@ void split_subpasses(int logR, PassParams& p) {
   for (int i = 0; i < nsub; ++i) p.q[i] = base + (i < extra ? 1 : 0);
 }
 
-// Latency mode: one or two small transforms (at most 8192 points in all) would
-// run on one or two SMs in a single pass, and an FP64 transform of 4096 points
-// then takes ~40 us on one SM (GB300 issues FP64 at 2 lanes per SM).  Two
-// passes of 128-point one-warp tiles (k_pass_lat, four points per thread)
-// spread the same work over 32-64 SMs.
-constexpr long long kLatencyMaxWork = 8192;
+// Latency mode: one or two small transforms (2^10..2^14 points, at most 16384
+// points in all) would run on 1-4 SMs in 4096-point tiles, and an FP64
+// transform of 4096 points then takes ~40 us on one SM (GB300 issues FP64 at 2
+// lanes per SM).  Two passes of 128-point one-warp tiles (k_pass_lat, four
+// points per thread, radix <= 2^7 per pass) spread the same work over 16-128
+// SMs.
+constexpr long long kLatencyMaxWork = 16384;
 constexpr int kLatencyTileLog = 7;  // kLatencyEPT points x 32 threads
 
 // tileLog: log2 of the complex elements per CTA tile (10..12); multi-pass
@@ -304,7 +305,7 @@ AxisPlan make_axis_plan(long long L, long long s, long long nlines, int lq_log,
   const int logL = ilog2((unsigned long long)L);
   const int maxPassLog = std::min(kMaxPassLog, tileLog - 2);
   std::vector<int> radix;
-  const bool latency = !full_tile && s == 1 && logL >= 10 && logL <= 12 &&
+  const bool latency = !full_tile && s == 1 && logL >= 10 && logL <= 2 * kLatencyTileLog &&
                        L * nlines <= kLatencyMaxWork;
   if (radices) {
     radix = *radices;
