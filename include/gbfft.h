@@ -268,6 +268,13 @@ int gbfft_correl_batch(const double* const* data1, const size_t* n1, const doubl
 int gbfft_correl_normalized(const double* data1, size_t n1, const double* data2, size_t n2,
                             double* ans, int fast, const gbfft_opts* opts);
 
+/* fourn (src/Fourn.rs:278 contract: row-major, nn[ndim-1] fastest) along the
+ * axes whose bits are set in `axes` (bit i = axis i) only: the local steps of
+ * an N-D transform split across ranks (the Python mirror's
+ * numrs_gb300.dist.fourn_sharded).  Every nn[i] a power of two >= 1. */
+int gbfft_fourn_axes(double* data, const size_t* nn, size_t ndim, unsigned long long axes,
+                     int isign, const gbfft_opts* opts);
+
 /* Four-step twiddle of a four1 of n points split across ranks (one GPU each;
  * the Python mirror's numrs_gb300.dist runs column transforms, this twiddle,
  * one all-to-all and row transforms).  data: `lines` lines of `len` complex

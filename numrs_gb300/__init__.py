@@ -35,7 +35,7 @@ __all__ = [
     "autocorrel", "magnitude_spectrum", "power_spectrum", "real_to_complex",
     "complex_to_real", "ConvlvError", "CorrelError", "GbfftError", "launch_count",
     "FFTBatch", "four1_many", "set_async", "profile", "profile_read", "four1_noalloc",
-    "four1_spectrum", "set_spectral_path", "fourfs", "twiddle_lines",
+    "four1_spectrum", "set_spectral_path", "fourfs", "twiddle_lines", "fourn_axes",
     "correl_normalized", "correl_normalized_fast", "autocorrel_fast", "ConvlvProcessor",
     "RealFTProcessor", "TwoFFTProcessor",
 ]
@@ -323,6 +323,30 @@ def fourn(data, nn, ndim, isign, form="fp64"):
     arr = (ctypes.c_size_t * max(len(nn), 1))(*nn)
     o = _opts([a], form)
     st = _lib.load().gbfft_fourn(a.ptr, arr, len(nn), ndim, isign, ctypes.byref(o))
+    if st == _lib.INVALID_ARG:
+        raise ValueError(_lib.last_error())
+    _check(st)
+
+
+def fourn_axes(data, nn, axes, isign, form="fp64"):
+    """fourn (row-major, ``src/Fourn.rs:278`` contract) along the listed axes
+    only (axis 0 slowest): the local steps of an N-D transform split across
+    ranks (``numrs_gb300.dist.fourn_sharded``)."""
+    a = _Arg(data, True)
+    nn = list(nn)
+    total = 1
+    for v in nn:
+        total *= int(v)
+    if a.size < 2 * total:
+        raise ValueError("data holds %d doubles, need %d" % (a.size, 2 * total))
+    mask = 0
+    for ax in axes:
+        if not 0 <= int(ax) < len(nn):
+            raise ValueError("axis %r out of range" % (ax,))
+        mask |= 1 << int(ax)
+    arr = (ctypes.c_size_t * max(len(nn), 1))(*nn)
+    o = _opts([a], form)
+    st = _lib.load().gbfft_fourn_axes(a.ptr, arr, len(nn), mask, isign, ctypes.byref(o))
     if st == _lib.INVALID_ARG:
         raise ValueError(_lib.last_error())
     _check(st)

@@ -57,6 +57,7 @@ SIGNATURES = {
     "gbfft_magnitude_spectrum": [_vp, _sz, _vp, _op],
     "gbfft_power_spectrum": [_vp, _sz, _vp, _op],
     "gbfft_twiddle_lines": [_vp, _sz, _sz, _sz, _sz, ctypes.c_int, _op],
+    "gbfft_fourn_axes": [_vp, ctypes.POINTER(_sz), _sz, ctypes.c_ulonglong, ctypes.c_int, _op],
     "gbfft_release": [],
     "gbfft_four1_noalloc": [_vp, _sz, ctypes.c_int, _vp],
     "gbfft_profile": [ctypes.c_int],

@@ -857,10 +857,12 @@ bool rlft3_twist_plan(const AxisPlan& base, int logU, int logV, AxisPlan& out) {
 // fourn on device data.  ex (3-D only): the rlft3 twist on the last axis
 // processed (axis 0, forward) or the first (the last axis, inverse), whose
 // plan is twist_plan.
+// axes: bit dd set = transform axis dd (default: every axis).
 int fourn_dev(Form f, double* d, const long long* nn, int ndim, int isign,
-              const AxisExtras* ex = nullptr, const AxisPlan* twist_plan = nullptr) {
+              const AxisExtras* ex = nullptr, const AxisPlan* twist_plan = nullptr,
+              unsigned long long axes = ~0ull) {
   for (int dd = ndim - 1; dd >= 0; --dd) {
-    if (nn[dd] <= 1) continue;
+    if (nn[dd] <= 1 || !((axes >> dd) & 1ull)) continue;
     const bool with = ex && ((ex->twist > 0 && dd == 0) || (ex->twist < 0 && dd == ndim - 1));
     TRY(run_axis(f, isign, with ? *twist_plan : nd_axis_plan(f, nn, ndim, dd), d, 1.0, nullptr, 0,
                  0, nullptr, with ? ex : nullptr));
@@ -1713,6 +1715,38 @@ int gbfft_fourn(double* data, const size_t* nn, size_t nn_len, size_t ndim, int 
   double* d;
   TRY(stage_inout(c, g.stage_a, data, 2 * total, &d));
   TRY(fourn_dev(c.form(), d, dims, (int)ndim, isign));
+  TRY(unstage(c, data, d, 2 * total));
+  return ss.finish(c);
+}
+
+// fourn along a subset of the axes: the local steps of an N-D transform split
+// across ranks (slabs of axis 0 transform the other axes, exchange, then axis
+// 0).  Every dimension a power of two >= 1; `axes` a non-empty bit set of
+// axes below ndim.
+int gbfft_fourn_axes(double* data, const size_t* nn, size_t ndim, unsigned long long axes,
+                     int isign, const gbfft_opts* opts) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Call c(opts);
+  TRY(check_form(c));
+  if (!nn || ndim == 0 || ndim > 16) return fail(GBFFT_INVALID_ARG, "fourn_axes: invalid dimensions");
+  if (isign != 1 && isign != -1) return fail(GBFFT_INVALID_ARG, "fourn_axes: isign must be 1 or -1");
+  if (axes == 0 || (ndim < 64 && (axes >> ndim) != 0))
+    return fail(GBFFT_INVALID_ARG, "fourn_axes: axes must name axes below ndim");
+  if (!data) return fail(GBFFT_INVALID_ARG, "fourn_axes: null data");
+  TRY(dev_aligned(c, "fourn_axes", {data}));
+  long long dims[16];
+  size_t total = 1;
+  for (size_t i = 0; i < ndim; ++i) {
+    if (!is_pow2(nn[i]) || ilog2(nn[i]) > kMaxAxisLog)
+      return fail(GBFFT_UNSUPPORTED_SIZE, "fourn_axes: nn[%zu]=%zu must be a power of two", i, nn[i]);
+    dims[i] = (long long)nn[i];
+    total *= nn[i];
+  }
+  TRY(init_locked(g.device));
+  StreamScope ss(c);
+  double* d;
+  TRY(stage_inout(c, g.stage_a, data, 2 * total, &d));
+  TRY(fourn_dev(c.form(), d, dims, (int)ndim, isign, nullptr, nullptr, axes));
   TRY(unstage(c, data, d, 2 * total));
   return ss.finish(c);
 }

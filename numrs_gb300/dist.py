@@ -28,10 +28,19 @@ step 4.  Between GPUs the exchanges are torch.distributed all_to_all_single
 `four1_sharded_local` runs P shares held by one process (one device) with the
 exchanges done as copies: the same steps and kernels, for single-GPU tests and
 for timing the local work.
+
+fourn (src/Fourn.rs:278 contract, row-major dims n0 x n1 x ...) over slabs:
+rank r holds the slabs i0 in [r n0/P, (r+1) n0/P) ("slabs0", a contiguous
+block of the array).  It transforms its slabs along axes 1.. (library:
+fourn_axes), one all-to-all regroups the array into slabs of axis 1
+("slabs1": rank r holds i1 in [r n1/P, (r+1) n1/P), all i0), and the ranks
+transform along axis 0.  A "slabs0" output takes one more all-to-all.
+`fourn_sharded` / `fourn_sharded_local` as above.
 """
 import numpy as np
 
-__all__ = ["split_sizes", "four1_sharded", "four1_sharded_local", "to_layout", "from_layout"]
+__all__ = ["split_sizes", "four1_sharded", "four1_sharded_local", "to_layout", "from_layout",
+           "fourn_sharded", "fourn_sharded_local", "to_slabs", "from_slabs"]
 
 LAYOUTS = ("columns", "rows", "block")
 
@@ -212,3 +221,115 @@ def from_layout(shares, N, layout):
         m = np.concatenate([p.reshape(N2 // P, N1, 2) for p in parts])  # [k2, k1]
         return np.ascontiguousarray(m.transpose(1, 0, 2)).reshape(-1)
     raise ValueError("unknown layout %r" % (layout,))
+
+
+# ---------------------------------------------------------------------------
+# fourn over slabs of axis 0
+# ---------------------------------------------------------------------------
+def _check_slabs(dims, P, isign, out_layout):
+    dims = [int(v) for v in dims]
+    if len(dims) < 2:
+        raise ValueError("fourn over slabs needs two or more dimensions")
+    if isign not in (1, -1):
+        raise ValueError("isign must be +1 or -1")
+    if out_layout not in ("slabs0", "slabs1"):
+        raise ValueError("out_layout is 'slabs0' or 'slabs1'")
+    if dims[0] % P or dims[1] % P:
+        raise ValueError("dims %s do not split over %d ranks along axes 0 and 1" % (dims, P))
+    return dims
+
+
+def _fourn_axes(t, dims, axes, isign, form):
+    from . import fourn_axes
+    fourn_axes(t, dims, axes, isign, form=form)
+
+
+def _slabs0_to_slabs1_send(x, dims, P):
+    """(n0/P, n1, rest) -> chunks (P, n0/P, n1/P, rest): chunk s holds the
+    i1 range of rank s."""
+    n0, n1 = dims[0], dims[1]
+    rest = x.numel() // (2 * (n0 // P) * n1)
+    return x.view(n0 // P, P, n1 // P, rest, 2).permute(1, 0, 2, 3, 4).contiguous()
+
+
+def _slabs1_to_slabs0_send(x, dims, P):
+    """(n0, n1/P, rest) -> chunks (P, n0/P, n1/P, rest): chunk s holds the
+    i0 range of rank s."""
+    n0, n1 = dims[0], dims[1]
+    rest = x.numel() // (2 * n0 * (n1 // P))
+    return x.view(P, n0 // P, n1 // P, rest, 2).contiguous()
+
+
+def _slabs0_from_recv(recv, dims, P):
+    """Chunks (P (from rank q: its i1 range), n0/P, n1/P, rest) -> (n0/P, n1, rest)."""
+    n0, n1 = dims[0], dims[1]
+    return recv.permute(1, 0, 2, 3, 4).reshape(-1)
+
+
+def fourn_sharded(share, dims, isign, out_layout="slabs1", form="fp64", group=None,
+                  transform=None):
+    """This rank's part of fourn of a row-major array of dims over the ranks of
+    `group`; `share` holds its slabs of axis 0 (a CUDA float64 tensor).
+    Returns its part in `out_layout`.  `transform(t, dims, axes, isign)`
+    replaces the library's fourn_axes (tests on hosts without a GPU)."""
+    import torch
+    import torch.distributed as dist
+    P = dist.get_world_size(group)
+    dims = _check_slabs(dims, P, isign, out_layout)
+    tf = transform or (lambda t, d, axes, sg: _fourn_axes(t, d, axes, sg, form))
+    local0 = [dims[0] // P] + dims[1:]
+    x = share.contiguous()
+    tf(x, local0, list(range(1, len(dims))), isign)
+    send = _slabs0_to_slabs1_send(x, dims, P)
+    recv = torch.empty_like(send)
+    dist.all_to_all_single(recv, send, group=group)
+    x = recv.reshape(-1)  # chunk q = rank q's i0 range: (n0, n1/P, rest) in order
+    local1 = [dims[0], dims[1] // P] + dims[2:]
+    tf(x, local1, [0], isign)
+    if out_layout == "slabs0":
+        send = _slabs1_to_slabs0_send(x, dims, P)
+        recv = torch.empty_like(send)
+        dist.all_to_all_single(recv, send, group=group)
+        x = _slabs0_from_recv(recv, dims, P)
+    return x
+
+
+def fourn_sharded_local(shares, dims, isign, out_layout="slabs1", form="fp64", transform=None):
+    """The same for P = len(shares) shares held by this process (exchanges as
+    copies)."""
+    import torch
+    P = len(shares)
+    dims = _check_slabs(dims, P, isign, out_layout)
+    tf = transform or (lambda t, d, axes, sg: _fourn_axes(t, d, axes, sg, form))
+    local0 = [dims[0] // P] + dims[1:]
+    xs = [s.contiguous() for s in shares]
+    for x in xs:
+        tf(x, local0, list(range(1, len(dims))), isign)
+    sends = [_slabs0_to_slabs1_send(x, dims, P) for x in xs]
+    xs = [torch.stack([sends[q][s] for q in range(P)]).reshape(-1) for s in range(P)]
+    local1 = [dims[0], dims[1] // P] + dims[2:]
+    for x in xs:
+        tf(x, local1, [0], isign)
+    if out_layout == "slabs0":
+        sends = [_slabs1_to_slabs0_send(x, dims, P) for x in xs]
+        xs = [_slabs0_from_recv(torch.stack([sends[q][s] for q in range(P)]), dims, P)
+              for s in range(P)]
+    return xs
+
+
+def to_slabs(x, dims, P, layout):
+    """A row-major array (2 prod(dims) doubles) as the P shares of a layout."""
+    dims = [int(v) for v in dims]
+    a = np.asarray(x, dtype=np.float64).reshape(dims + [2])
+    ax = 0 if layout == "slabs0" else 1
+    return [np.ascontiguousarray(b).reshape(-1) for b in np.split(a, P, axis=ax)]
+
+
+def from_slabs(shares, dims, layout):
+    dims = [int(v) for v in dims]
+    P = len(shares)
+    ax = 0 if layout == "slabs0" else 1
+    shp = list(dims) + [2]
+    shp[ax] //= P
+    parts = [np.asarray(s, dtype=np.float64).reshape(shp) for s in shares]
+    return np.ascontiguousarray(np.concatenate(parts, axis=ax)).reshape(-1)

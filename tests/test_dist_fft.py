@@ -1,6 +1,7 @@
-"""The sharded four1 (numrs_gb300.dist): four-step schedule with one
-all-to-all between the column and the row transforms, on two gloo ranks on
-the CPU.  The GPU library calls of the local steps are replaced here by numpy
+"""The sharded transforms of numrs_gb300.dist on two gloo ranks on the CPU:
+four1 (four-step schedule, one all-to-all between the column and the row
+transforms) and fourn over slabs of axis 0 (one all-to-all between the
+transforms of the other axes and axis 0).  The GPU library calls of the local steps are replaced here by numpy
 stand-ins (transform = four1's sign convention, twiddle = its definition), so
 the test checks the layouts, the exchanges and the twiddle exponents; the
 GPU test runs the same steps with the library's kernels.  Reference
@@ -119,3 +120,79 @@ def test_layout_round_trip_and_split():
         D.split_sizes(1 << 4, 8)
     with pytest.raises(ValueError):
         D.split_sizes(3 << 4, 2)
+
+
+def _fourn_np_axes(t, dims, axes, isign):
+    """fourn's transform (exp(isign 2 pi i ...), unnormalised) along `axes`."""
+    import torch
+    a = t.numpy().reshape(list(dims) + [2])
+    c = a[..., 0] + 1j * a[..., 1]
+    for ax in axes:
+        c = np.fft.ifft(c, axis=ax) * dims[ax] if isign > 0 else np.fft.fft(c, axis=ax)
+    out = np.stack([c.real, c.imag], axis=-1)
+    t.copy_(torch.from_numpy(np.ascontiguousarray(out).reshape(-1)))
+
+
+def _fourn_rank_main(rank, world, port, dims, isign, lout, x, q):
+    os.environ.update({"MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    sys.path.insert(0, ROOT)
+    import torch
+    import torch.distributed as dist
+    from numrs_gb300 import dist as D
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    share = torch.from_numpy(D.to_slabs(x, dims, world, "slabs0")[rank].copy())
+    out = D.fourn_sharded(share, dims, isign, out_layout=lout, transform=_fourn_np_axes)
+    q.put((rank, out.numpy().copy()))
+    dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("dims", [(8, 4, 16), (4, 8), (2, 2, 4, 8)])
+@pytest.mark.parametrize("lout", ["slabs1", "slabs0"])
+def test_sharded_fourn_two_gloo_ranks(dims, lout):
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    from numrs_gb300 import dist as D
+    world = 2
+    n = int(np.prod(dims))
+    x = np.random.default_rng(79).standard_normal(2 * n)
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_fourn_rank_main, args=(r, world, port, list(dims), -1, lout, x, q))
+             for r in range(world)]
+    for p in procs:
+        p.start()
+    got = dict(q.get(timeout=120) for _ in range(world))
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    y = D.from_slabs([got[r] for r in range(world)], dims, lout)
+    ref = np.zeros_like(x)
+    import torch as T
+    t = T.from_numpy(x.copy())
+    _fourn_np_axes(t, list(dims), list(range(len(dims))), -1)
+    ref = t.numpy()
+    assert np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("P", [1, 2, 4])
+def test_sharded_fourn_local_emulation_numpy(P):
+    pytest.importorskip("torch")
+    import torch
+    from numrs_gb300 import dist as D
+    dims = [8, 16, 4]
+    n = int(np.prod(dims))
+    x = np.random.default_rng(80).standard_normal(2 * n)
+    t = torch.from_numpy(x.copy())
+    _fourn_np_axes(t, dims, [0, 1, 2], 1)
+    ref = t.numpy()
+    for lout in ("slabs1", "slabs0"):
+        shares = [torch.from_numpy(s.copy()) for s in D.to_slabs(x, dims, P, "slabs0")]
+        outs = D.fourn_sharded_local(shares, dims, 1, out_layout=lout, transform=_fourn_np_axes)
+        y = D.from_slabs([o.numpy() for o in outs], dims, lout)
+        assert np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
+    with pytest.raises(ValueError):
+        D.fourn_sharded_local(shares, [n], 1)  # one dimension: nothing to split
+    if P > 1:
+        with pytest.raises(ValueError):
+            D.fourn_sharded_local(shares, [P // 2, 4 * P, 8], 1)  # axis 0 does not split

@@ -1,9 +1,11 @@
-"""The sharded four1 (numrs_gb300.dist) with the library's kernels on one
-GPU: the four-step schedule's local transforms (four1_many), the twiddle
-kernel (gbfft_twiddle_lines) and the exchanges, for P = 1, 2 and 4 shares
-held by one process, and the torch.distributed driver on a one-rank NCCL
-group.  Results must match the oracle's four1 (src/FFT_1.rs:5-107) or the
-single-GPU FP64 four1 within the FP64 bar."""
+"""The sharded transforms (numrs_gb300.dist) with the library's kernels on
+one GPU.  four1: the four-step schedule's local transforms (four1_many), the
+twiddle kernel (gbfft_twiddle_lines) and the exchanges, for P = 1, 2 and 4
+shares held by one process, and the torch.distributed driver on a one-rank
+NCCL group.  fourn over slabs: the axis-subset transform (gbfft_fourn_axes)
+and the slab exchange.  Results must match the oracle's four1
+(src/FFT_1.rs:5-107) and fourn (src/Fourn.rs:278 contract), or the
+single-GPU FP64 transforms, within the FP64 bar."""
 import os
 import socket
 
@@ -128,3 +130,59 @@ def test_sharded_torch_distributed_one_rank(env):
         assert rel_l2(out.cpu().numpy(), ref) <= 1e-12
     finally:
         dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("axes", [[0], [1], [2], [1, 2], [0, 2], [0, 1, 2]])
+@pytest.mark.parametrize("form", ["fp64", "fp32"])
+def test_fourn_axes(env, axes, form):
+    """gbfft_fourn_axes against numpy's FFT along the same axes (fourn's sign:
+    isign = -1 is numpy's forward transform)."""
+    nr, D = env
+    dims = [8, 32, 64]
+    n = int(np.prod(dims))
+    x = np.random.default_rng(6400).standard_normal(2 * n)
+    d = x.copy()
+    nr.fourn_axes(d, dims, axes, -1, form=form)
+    c = (x[0::2] + 1j * x[1::2]).reshape(dims)
+    for ax in axes:
+        c = np.fft.fft(c, axis=ax)
+    ref = np.stack([c.real, c.imag], axis=-1).reshape(-1)
+    e = rel_l2(d, ref)
+    assert e <= (1e-12 if form == "fp64" else 1e-6), "fourn_axes %s %s rel-L2 %.3e" % (axes, form, e)
+
+
+@pytest.mark.parametrize("P", [1, 2, 4])
+@pytest.mark.parametrize("lout", ["slabs1", "slabs0"])
+def test_fourn_sharded_local_vs_oracle(env, P, lout):
+    import torch
+    import oracle as O
+    nr, D = env
+    dims = [16, 32, 64]
+    n = int(np.prod(dims))
+    x = np.random.default_rng(6500 + P).standard_normal(2 * n)
+    ref = x.copy()
+    assert O.fourn(ref, dims, 1) == 0
+    shares = [torch.from_numpy(s.copy()).cuda() for s in D.to_slabs(x, dims, P, "slabs0")]
+    outs = D.fourn_sharded_local(shares, dims, 1, out_layout=lout)
+    torch.cuda.synchronize()
+    y = D.from_slabs([o.cpu().numpy() for o in outs], dims, lout)
+    e = rel_l2(y, ref)
+    assert e <= 1e-12, "fourn over %d slabs rel-L2 %.3e" % (P, e)
+
+
+def test_fourn_sharded_local_c4(env):
+    """fourn of 256 x 256 x 512 over 4 slabs against the single-GPU fourn."""
+    import torch
+    from numrs_gb300 import workloads as W
+    nr, D = env
+    dims = [256, 256, 512]
+    n = int(np.prod(dims))
+    x = torch.from_numpy(W.normal(6600, 2 * n)).cuda()
+    ref = x.clone()
+    nr.fourn(ref, dims, 3, 1)
+    shares = list(x.view(4, -1).clone().unbind(0))
+    outs = D.fourn_sharded_local(shares, dims, 1, out_layout="slabs0")
+    y = torch.cat(outs)
+    torch.cuda.synchronize()
+    e = float(torch.linalg.vector_norm(y - ref) / torch.linalg.vector_norm(ref))
+    assert e <= 1e-12, "fourn C4 over 4 slabs rel-L2 %.3e" % e
