@@ -76,7 +76,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large",
                     choices=["large", "convlv", "four1", "batch", "fourn", "rlft3", "c1", "convbatch",
-                             "peaks", "sharded"])
+                             "peaks", "sharded", "link"])
     ap.add_argument("--form", default="fp64", choices=["fp64", "df64", "fp32", "tc32"])
     ap.add_argument("--no-forms", action="store_true", help="skip the extra precision forms")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched target in the default line")
@@ -1221,6 +1221,56 @@ def run_sharded(args, world, rank, local):
     return line
 
 
+def run_link(args, world, rank, local):
+    """CPU-GPU link bandwidth through torch copies of a 4 GiB pinned host
+    tensor (cudaMemcpyAsync), timed with CUDA events: host to device, device
+    to host, and both at once on two streams.  The first and last passes of
+    a transform of host data move its bytes over this link.  Not an FFT
+    workload."""
+    import torch
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    nbytes = 4 << 30
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    h2 = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    d2 = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def timed(fn, reps=3):
+        best = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            torch.cuda.synchronize()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        return best
+
+    def both():
+        with torch.cuda.stream(s1):
+            d.copy_(h, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+
+    for _ in range(max(args.warmup, 1)):
+        d.copy_(h, non_blocking=True)
+    res = {"h2d_gbs": nbytes / timed(lambda: d.copy_(h, non_blocking=True)) / 1e6,
+           "d2h_gbs": nbytes / timed(lambda: h.copy_(d, non_blocking=True)) / 1e6,
+           "both_at_once_gbs_each_way": nbytes / timed(both) / 1e6}
+    if rank != 0:
+        return None
+    return {"metric": "CPU-GPU link GB/s (pinned host memory)", "value": res["h2d_gbs"],
+            "unit": "GB/s", "n_gpus": world, "higher_is_better": True, "dtype": "u8",
+            "data": "4 GiB pinned host tensors", "config": {"workload": "torch copies host <-> device"},
+            "link": res}
+
+
 def run_convbatch(args, world, rank, local):
     """convlv_batch: 64 convolutions of N=2^16 reals with one 257-tap response
     (the C2 response construction at N=2^16), one library call per step; the
@@ -1293,7 +1343,7 @@ def main():
         dist.init_process_group("nccl")
     fn = {"large": run_large, "four1": run_four1, "batch": run_batch, "fourn": run_nd,
           "rlft3": run_nd, "c1": run_c1, "convbatch": run_convbatch,
-          "peaks": run_peaks, "sharded": run_sharded}.get(args.workload)
+          "peaks": run_peaks, "sharded": run_sharded, "link": run_link}.get(args.workload)
     if fn is None:
         run_convlv(args, world, rank, local)
     else:
