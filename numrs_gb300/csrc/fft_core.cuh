@@ -501,6 +501,46 @@ __device__ __forceinline__ void load_tile_raw(const PassParams& p, long long lin
 
 // One full tile from global memory.  L2_ONLY loads bypass L1 (data written by
 // other CTAs of the same launch).
+// Stage a thread's EPT raw elements into the tile with their inter-pass
+// twiddles.  The twiddles are gathered in groups of eight, all loads of a
+// group issued before any is used, so that a thread waits on one table
+// round trip per group instead of one per element; the exponent-0 entries
+// (j mod Ns = 0 or r = 0) read the table's exact 1 + 0i.
+template <class F, int SG, int IN, int T, int EPT>
+__device__ __forceinline__ void stage_tile(const PassParams& p, long long line0, long long j0,
+                                           int tid, const typename IOElem<IN>::T (&raw)[EPT],
+                                           typename F::S* sm) {
+  using C = typename F::C;
+  constexpr int G = EPT >= 8 ? 8 : EPT;
+  constexpr int sh = F::kPadShift;
+  const int cs = col_stride(p.logR, sh);
+  const bool tw_on = p.logNs > 0;
+  const int logS = p.logNs + p.logR;
+#pragma unroll
+  for (int g0 = 0; g0 < EPT; g0 += G) {
+    C w[G];
+    if (tw_on) {
+#pragma unroll
+      for (int i = 0; i < G; ++i) {
+        int c, r;
+        elem_cr(tid + (g0 + i) * T, p.in_rcontig, p.logR, p.logC, c, r);
+        const long long j = (p.mode == 0) ? j0 + c : j0;
+        const unsigned jm = (unsigned)(j & (p.Ns - 1));
+        w[i] = twiddle<F>(p.tw, logS, jm * (unsigned)r, SG);  // jm * r < Ns * R <= L
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+      int c, r;
+      elem_cr(tid + (g0 + i) * T, p.in_rcontig, p.logR, p.logC, c, r);
+      const long long line = (p.mode == 0) ? line0 : line0 + c;
+      C v = (line < p.nlines) ? gload<F, IN>(&raw[g0 + i], 0) : F::from_d(0.0, 0.0);
+      if (tw_on) v = F::mul(v, w[i]);
+      sm[c * cs + pidx(r, sh)] = F::to_s(v);
+    }
+  }
+}
+
 template <class F, int SG, int IN, int OUT, int T, bool L2_ONLY, int EPT = kEPT>
 __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
                                           typename F::S* sm, int tid) {
@@ -509,8 +549,7 @@ __device__ __forceinline__ void pass_tile(const PassParams& p, long long tile,
   tile_origin(p, tile, line0, j0);
   IE raw[EPT];
   load_tile_raw<IE, IN, T, L2_ONLY, EPT>(p, line0, j0, tid, raw);
-#pragma unroll
-  for (int k = 0; k < EPT; ++k) stage_elem<F, SG, IN>(p, line0, j0, tid + k * T, raw[k], sm);
+  stage_tile<F, SG, IN, T, EPT>(p, line0, j0, tid, raw, sm);
   __syncthreads();
   tile_compute_store<F, SG, OUT, T, EPT>(p, line0, j0, sm, tid);
 }
