@@ -122,6 +122,11 @@ long long gbfft_launch_count(int reset);
  *                                 two passes on four-CTA clusters (also
  *                                 GBFFT_CLUSTER_PASS=1 at start-up), 0: as
  *                                 three per-CTA passes (the default, faster)
+ *   GBFFT_DEBUG_TOP_TWIDDLES      1: the last pass of a long FP64 axis
+ *                                 reads its twiddles from a dense copy of
+ *                                 their level (the default), 0: as products
+ *                                 of two table entries (also
+ *                                 GBFFT_TOP_TWIDDLES=0 at start-up)
  * The batch settings drop the cached batch plan.  Nothing here hangs or
  * faults a GPU: every device wait stays bounded. */
 enum {
@@ -131,7 +136,8 @@ enum {
   GBFFT_DEBUG_BATCH_FIRST_RADIX_DELTA = 4,
   GBFFT_DEBUG_FUSED_TWIST = 5,
   GBFFT_DEBUG_TC_UMMA = 6,
-  GBFFT_DEBUG_CLUSTER_PASS = 7
+  GBFFT_DEBUG_CLUSTER_PASS = 7,
+  GBFFT_DEBUG_TOP_TWIDDLES = 8
 };
 int gbfft_debug_set(int key, long long value);
 int gbfft_profile(int enable);  /* also clears the records */

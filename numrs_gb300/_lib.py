@@ -75,6 +75,7 @@ DEBUG_BATCH_FIRST_RADIX_DELTA = 4
 DEBUG_FUSED_TWIST = 5
 DEBUG_TC_UMMA = 6
 DEBUG_CLUSTER_PASS = 7
+DEBUG_TOP_TWIDDLES = 8
 
 _lib = None
 

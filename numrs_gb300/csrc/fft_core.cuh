@@ -71,6 +71,7 @@ __device__ __forceinline__ typename F::C twiddle(const Twiddles& tw, int logS, u
   using TW = typename F::TW;
   const TW* dense = reinterpret_cast<const TW*>(tw.dense);
   if (logS <= tw.dense_log) return F::ld_tw(dense + ((1u << logS) + e), sg);
+  if (logS == tw.top_log) return F::ld_tw(reinterpret_cast<const TW*>(tw.top) + e, sg);
   const TW* part = reinterpret_cast<const TW*>(tw.partial);
   typename F::C hi = F::ld_tw(dense + ((1u << (logS - kPartialLog)) + (e >> kPartialLog)), sg);
   typename F::C lo = F::ld_tw(part + ((unsigned)(logS - tw.dense_log - 1) * kPartial +

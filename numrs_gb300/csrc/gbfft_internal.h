@@ -44,6 +44,10 @@ struct Twiddles {
   const void* dense = nullptr;
   const void* partial = nullptr;
   int dense_log = kDenseLog;  // largest level held densely
+  // optional dense copy of one level above dense_log (the last pass of a
+  // long FP64 or double-float axis): entry e = w_{2^top_log}^e; 0 = none
+  const void* top = nullptr;
+  int top_log = 0;
 };
 
 // One Stockham pass over an axis.  The axis has length L and stride s
@@ -171,6 +175,7 @@ cudaError_t launch_pass_lat(Form f, int sign, IOType in, IOType out, const PassP
 cudaError_t launch_pass_cl_f32(int sign, IOType in, IOType out, const PassParams& p, int threads,
                                cudaStream_t st);
 cudaError_t launch_twiddles(Form f, void* dense, void* partial, int dense_log, cudaStream_t st);
+cudaError_t launch_twiddle_level(Form f, void* level, int logS, cudaStream_t st);
 
 // spectral / real-transform kernels (spectral.cu)
 struct SpecArgs {

@@ -55,6 +55,30 @@ __global__ void k_twiddles(typename F::TW* dense, typename F::TW* partial, int d
   }
 }
 
+// One dense level: entry e = exp(+2 pi i e / 2^logS), e < 2^logS.
+template <class F>
+__global__ void k_twiddle_level(typename F::TW* level, int logS) {
+  const size_t n = (size_t)1 << logS;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    double c, s;
+    if (e == 0) {
+      c = 1.0; s = 0.0;
+    } else {
+      sincospi(2.0 * (double)e / (double)n, &s, &c);
+    }
+    put_tw<F>(level, e, c, s);
+  }
+}
+
+cudaError_t launch_twiddle_level(Form f, void* level, int logS, cudaStream_t st) {
+  dim3 g(152 * 16), b(256);
+  if (f == FORM_F64) k_twiddle_level<F64><<<g, b, 0, st>>>((d2*)level, logS);
+  else if (f == FORM_DF64) k_twiddle_level<DF64><<<g, b, 0, st>>>((f4*)level, logS);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
 cudaError_t launch_twiddles(Form f, void* dense, void* partial, int dense_log, cudaStream_t st) {
   dim3 g(1024), b(256);
   if (f == FORM_F64) k_twiddles<F64><<<g, b, 0, st>>>((d2*)dense, (d2*)partial, dense_log);

@@ -735,3 +735,31 @@ def test_convlv_device_paths(nr):
     st, ref_b = O.convlv(xb, r, 1)
     got = nr.convlv(torch.from_numpy(xb).cuda(), torch.from_numpy(r).cuda(), 1).cpu().numpy()
     assert_fp64_close(got, ref_b, 22, "device convlv 2^22")
+
+
+@pytest.mark.parametrize("form", ["fp64", "df64"])
+@pytest.mark.parametrize("log2n", [21, 22])
+@pytest.mark.parametrize("isign", [1, -1])
+def test_top_twiddle_level(nr, form, log2n, isign):
+    """The last pass of a long FP64 axis reads its twiddles from a dense copy
+    of their level (the default) or forms them as products of two table
+    entries (debug key off; the double-float form always does): both within
+    the FP64 bar of the oracle's four1."""
+    from numrs_gb300 import _lib as L
+    lib = L.load()
+    nn = 1 << log2n
+    x = W.normal(8000 + log2n, 2 * nn)
+    ref = x.copy()
+    O.four1(ref, nn, isign)
+    got = {}
+    for top in (1, 0):
+        assert lib.gbfft_debug_set(L.DEBUG_TOP_TWIDDLES, top) == L.OK
+        try:
+            d = x.copy()
+            nr.four1(d, nn, isign, form=form)
+        finally:
+            lib.gbfft_debug_set(L.DEBUG_TOP_TWIDDLES, 1)
+        check(d, ref, log2n, form, "four1 2^%d %s top=%d" % (log2n, form, top))
+        got[top] = d
+    # the two twiddle paths differ by the rounding of one product
+    assert rel_l2(got[1], got[0]) <= 1e-13
