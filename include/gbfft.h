@@ -71,7 +71,8 @@ const char* gbfft_last_error(void);      /* message of the last failure      */
 int gbfft_version(void);                 /* 10000*major + 100*minor + patch  */
 /* Device scratch currently held by the library, in bytes. */
 size_t gbfft_scratch_bytes(void);
-/* Free cached plans, graphs and scratch (tables are kept). */
+/* Free cached plans, graphs, scratch and the dense copies of large twiddle
+ * levels (the base twiddle tables are kept). */
 int gbfft_release(void);
 /* Autotuner (no counterpart in the crate): when enabled, the first plan of
  * each axis shape and form times candidate tile sizes on a scratch array and

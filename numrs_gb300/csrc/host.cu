@@ -1446,6 +1446,12 @@ int gbfft_release(void) {
   }
   g_plans.clear();
   batch_plan_free(g_batch);
+  // the dense copies of large twiddle levels are as large as the data they
+  // served; they are rebuilt on the next transform that needs one
+  for (auto& m : g.tw_top) {
+    for (auto& kv : m) cudaFree(kv.second);
+    m.clear();
+  }
   return GBFFT_OK;
 }
 

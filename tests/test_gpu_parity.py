@@ -763,3 +763,8 @@ def test_top_twiddle_level(nr, form, log2n, isign):
         got[top] = d
     # the two twiddle paths differ by the rounding of one product
     assert rel_l2(got[1], got[0]) <= 1e-13
+    # gbfft_release frees the dense level; the next transform rebuilds it
+    assert lib.gbfft_release() == L.OK
+    d = x.copy()
+    nr.four1(d, nn, isign, form=form)
+    assert np.array_equal(d, got[1])
