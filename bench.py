@@ -61,6 +61,12 @@ NCU_TRAFFIC = {
 }
 
 
+# FP64 pipe activity (sm__pipe_fp64_cycles_active, % of active cycles) of the
+# FP64 pass kernel, passes 1-3 of four1 2^26, from one ncu capture: fixed,
+# not measured by this run.
+NCU_FP64_PIPE_BUSY = [0.841, 0.839, 0.835]
+
+
 def traffic_of(workload, form):
     t = NCU_TRAFFIC.get((workload, form))
     if t is None:
@@ -372,7 +378,12 @@ def run_large(args, world, rank, local):
                                       (FP64_PEAK_TFLOPS if form == "fp64" else FP32_PEAK_TFLOPS))
                              if pass_ms else 0.0,
                              "note": "nominal 5 N log2 R per radix-R pass over the pass kernel's "
-                                     "event time; peaks from the DFMA / FFMA loop probes"},
+                                     "event time; peaks from the DFMA / FFMA loop probes",
+                             "fp64_pipe_busy": NCU_FP64_PIPE_BUSY if form == "fp64" else None,
+                             "fp64_pipe_busy_note": "ncu sm__pipe_fp64_cycles_active of the same "
+                             "pass kernel on four1 2^26 (fixed capture, not measured in this "
+                             "run); nominal flops undercount the pipe because most FP64 "
+                             "instructions are DADD/DMUL, not DFMA" if form == "fp64" else None},
         "kernels": {"pass": {"ms": pass_ms, "launches": pass_n}},
         "accuracy": {"rel_l2_vs_fp64_form": acc_main},
         "forms": forms,
