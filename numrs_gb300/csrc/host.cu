@@ -38,7 +38,7 @@ struct ProfRec {
 
 struct Ctx {
   bool inited = false;
-  int device = 0;
+  int device = -1;  // bound at the first call (-1: not yet)
   cudaStream_t stream = nullptr;  // library stream
   cudaStream_t cur = nullptr;     // stream of the call in progress
   // Calls share the library's work buffers.  An asynchronous device call
@@ -157,13 +157,28 @@ int ensure(DevBuf& b, size_t bytes) {
   return GBFFT_OK;
 }
 
+// The library binds to one device: `device` when gbfft_init names one (>= 0),
+// else the device current on the calling thread at its first call (one
+// process per GPU: each rank selects its device before its first call).
+// Later calls run their work on that device whatever the calling thread's
+// current device is (StreamScope), and leave the caller's current device as
+// they found it.
 int init_locked(int device) {
   if (g.inited) return GBFFT_OK;
   int n = 0;
   cudaError_t e = cudaGetDeviceCount(&n);
   if (e != cudaSuccess || n == 0)
     return fail(GBFFT_CUDA_ERROR, "no CUDA device: %s", cudaGetErrorString(e));
-  CK(cudaSetDevice(device));
+  int cur = 0;
+  CK(cudaGetDevice(&cur));
+  if (device < 0) device = cur;
+  if (device >= n) return fail(GBFFT_INVALID_ARG, "init: device %d of %d", device, n);
+  struct Restore {
+    int dev;
+    bool on;
+    ~Restore() { if (on) cudaSetDevice(dev); }
+  } restore{cur, device != cur};
+  if (device != cur) CK(cudaSetDevice(device));
   CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&g.order_ev, cudaEventDisableTiming));
   g.cur = g.stream;
@@ -768,7 +783,21 @@ int check_form(const Call& c) {
 // Calls on a stream that is capturing a CUDA graph neither wait on nor record
 // the ordering event: an event recorded outside a capture cannot be waited on
 // inside it, and the graph itself orders what it captures.
+// Makes the library's device current for the duration of a call and puts the
+// caller's back afterwards.
+struct DeviceGuard {
+  int prev = -1;
+  DeviceGuard() {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != g.device) cudaSetDevice(g.device);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0 && prev != g.device) cudaSetDevice(prev);
+  }
+};
+
 struct StreamScope {
+  DeviceGuard dg;
   bool capturing = false;
   explicit StreamScope(const Call& c) {
     g.cur = c.dev() ? (cudaStream_t)c.o->stream : g.stream;
@@ -1437,6 +1466,7 @@ size_t gbfft_scratch_bytes(void) {
 int gbfft_release(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g.inited) return GBFFT_OK;
+  DeviceGuard dg;
   cudaDeviceSynchronize();
   g.order_pending = false;
   for (DevBuf* b : {&g.scratch, &g.work, &g.stage_a, &g.stage_b, &g.stage_c, &g.ptrtab}) {
