@@ -73,6 +73,14 @@ def test_argument_errors_need_no_gpu(lib):
     assert lib.gbfft_rlft3(p, p, 2, 2, 2, 0, None) == L.INVALID_ARG
     msg = L.last_error()
     assert "isign" in msg
+    # the local steps of the sharded transforms
+    dims = (ctypes.c_size_t * 3)(2, 4, 8)
+    assert lib.gbfft_fourn_axes(p, dims, 3, 0, 1, None) == L.INVALID_ARG      # no axis
+    assert lib.gbfft_fourn_axes(p, dims, 3, 1 << 3, 1, None) == L.INVALID_ARG  # axis 3 of 3
+    assert lib.gbfft_fourn_axes(p, dims, 3, 1, 2, None) == L.INVALID_ARG      # isign
+    bad = (ctypes.c_size_t * 2)(3, 4)
+    assert lib.gbfft_fourn_axes(p, bad, 2, 1, 1, None) == L.UNSUPPORTED_SIZE
+    assert lib.gbfft_twiddle_lines(p, 2, 4, 0, 16, 1, None) == L.INVALID_ARG  # host data
 
 
 def test_python_mirror_raises_reference_errors(lib):
