@@ -68,7 +68,8 @@ typedef struct {
 /* Library control ------------------------------------------------------- */
 /* Optional: binds the library to `device`.  Without it (or with -1) the first
  * call binds it to the device current on the calling thread.  Every later
- * call runs on that device and leaves the caller's current device as it was. */
+ * call runs on that device and leaves the caller's current device as it was.
+ * Naming another device once bound is GBFFT_INVALID_ARG. */
 int gbfft_init(int device);
 const char* gbfft_last_error(void);      /* message of the last failure      */
 int gbfft_version(void);                 /* 10000*major + 100*minor + patch  */

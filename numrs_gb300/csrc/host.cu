@@ -1451,6 +1451,8 @@ extern "C" {
 
 int gbfft_init(int device) {
   std::lock_guard<std::mutex> lk(g_mu);
+  if (g.inited && device >= 0 && device != g.device)
+    return fail(GBFFT_INVALID_ARG, "init: the library is bound to device %d already", g.device);
   return init_locked(device);
 }
 
