@@ -137,3 +137,26 @@ def test_twiddle_table_allocation_failure_leaves_no_half_table(env):
             assert_fp64_close(d, ref, 12, "four1 %s after failed allocations" % form)
         else:
             assert np.linalg.norm(d - ref) / np.linalg.norm(ref) <= 1e-6
+
+
+def test_init_binds_one_device():
+    """The library binds to the calling thread's current device at its first
+    call (or to the device gbfft_init names); naming another device later is
+    an argument error, and the bound device keeps working."""
+    torch = pytest.importorskip("torch")
+    from numrs_gb300 import _lib as L
+    from numrs_gb300 import build
+    build.build()
+    lib = L.load()
+    cur = torch.cuda.current_device()
+    assert lib.gbfft_init(-1) == L.OK
+    assert lib.gbfft_init(cur) == L.OK
+    assert lib.gbfft_init(cur + 1) == L.INVALID_ARG
+    assert "bound to device" in L.last_error()
+    import numrs_gb300 as nr
+    x = np.random.default_rng(11).standard_normal(2 * 64)
+    d = x.copy()
+    nr.four1(d, 64, 1)
+    c = x[0::2] + 1j * x[1::2]
+    ref = np.fft.ifft(c) * 64
+    assert np.allclose(d[0::2] + 1j * d[1::2], ref, rtol=0, atol=1e-12 * np.abs(ref).max())
