@@ -1,5 +1,6 @@
-"""The autotuner of the persistent batch launch (the benchmark spec's batched
-path: "radix, tile and threads-per-transform chosen by an autotuner").
+"""The autotuner of the persistent batch launch: for every bin of the batch
+it chooses the radix split of two-pass transforms and the resident CTAs per
+SM (the batch kernel's tile and threads per transform).
 
 Every schedule it may choose is checked for correctness against the oracle
 (the two-pass bins' first radix shifted by -2..+2), and a tuning run in a
